@@ -1,0 +1,260 @@
+/*
+ * nwgb.h — C ABI of the GB300 nematic-worm step engine (libnwgb.so).
+ *
+ * One simulation step of self-propelled bead-spring filaments ("worms"),
+ * optionally coupled to a stochastic-rotation-dynamics (SRD) solvent:
+ *
+ *   integrate(r, v | f, f_old) -> [reverse] -> Langevin -> bonded (bend,
+ *   tangents, [bond, drive]) -> cell hash -> stable sort -> cell bounds ->
+ *   pair forces -> [every srd_gap steps: SRD stream + rotate-collide]
+ *
+ * This is the order of ParticleSystem::update in the reference
+ * (simulation/particleSystem.cpp:249-339) and of its SRD sub-step
+ * (simulation/particleSystem.cpp:341-413).
+ *
+ * Two pair-force models share one kernel skeleton:
+ *   NW_MODEL_WCA_WORMS  WCA Lennard-Jones between beads, harmonic bonds to
+ *                       chain neighbours, k(1-cos) bending, tangent drive
+ *                       F_act * unit(r_{i+1} - r_i), Langevin noise
+ *                       sqrt(2 gamma kT / dt).  Force laws of the archived
+ *                       engine (archived/vs_solution/fluid_substrate/
+ *                       NWDeviceFunctions.h:65-76, NWWormsKernel_InternalForce.h:37-59
+ *                       and 196-214, NWWormsKernel_BondBending.h:31-80,
+ *                       NWWormsKernel_DriveForce.h:21-34, NWWormsParameters.h:135-156).
+ *   NW_MODEL_REF_DEM    The modern engine's collideFilaments semantics:
+ *                       DEM spring/dashpot/shear contact, Hookean bond found
+ *                       through the cell list, extensile drive between
+ *                       anti-aligned beads, noise sqrt(2 gamma kT)
+ *                       (simulation/particles_kernel_impl.cuh:426-556, 694-744).
+ *
+ * Every entry point returns an nw_status; nothing in the library calls exit().
+ * State arrays are float4 (x, y, z, w) per particle, the reference layout
+ * (simulation/particleSystem.cpp:197-211): position.w = radius,
+ * velocity.w = mass.
+ */
+#ifndef NWGB_H
+#define NWGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NW_ABI_VERSION 1u
+
+typedef int nw_status;
+enum {
+    NW_OK = 0,
+    NW_ERR_CUDA = 1,          /* a CUDA runtime call failed */
+    NW_ERR_INVALID = 2,       /* bad argument or configuration */
+    NW_ERR_CELL_OVERFLOW = 3, /* a cell held more particles than a kernel's capacity */
+    NW_ERR_NONFINITE = 4,     /* a non-finite position or force was produced */
+    NW_ERR_TIMEOUT = 5,       /* a bounded device wait gave up */
+    NW_ERR_NOMEM = 6,         /* device or host allocation failed */
+    NW_ERR_UNSUPPORTED = 7,   /* feature not available in this configuration */
+    NW_ERR_NO_DEVICE = 8      /* no CUDA device visible */
+};
+
+/* Device error word bits (read with nw_error_word). */
+enum {
+    NW_EFLAG_NONFINITE = 1u << 0,
+    NW_EFLAG_CELL_OVERFLOW = 1u << 1,
+    NW_EFLAG_TIMEOUT = 1u << 2,
+    NW_EFLAG_BAD_INDEX = 1u << 3
+};
+
+typedef enum { NW_MODEL_WCA_WORMS = 0, NW_MODEL_REF_DEM = 1 } nw_model;
+
+/* Same numeric values as the reference's BoundaryType
+ * (simulation/particles_kernel.cuh:18-23). */
+typedef enum { NW_PERIODIC = 0, NW_WALL = 1, NW_WALL_NO_SLIP = 2 } nw_boundary;
+
+/* Cell-hash wrap rule.  NW_HASH_MASK is the reference's power-of-two mask
+ * (simulation/particles_kernel_impl.cuh:252-258); NW_HASH_MODULO wraps
+ * periodic axes with a true modulo and clamps wall axes. */
+typedef enum { NW_HASH_MODULO = 0, NW_HASH_MASK = 1 } nw_hash_mode;
+
+/* SRD cell thermostat.
+ *  NONE      no velocity rescaling.
+ *  REF_LAB   the reference's isokinetic rule: every particle of a cell is
+ *            scaled in the lab frame so that the cell's total kinetic energy
+ *            equals kT (simulation/particles_kernel_impl.cuh:605-637); it
+ *            runs before the cell mean is taken.
+ *  CELL_REL  relative velocities (v - u_cell) are rescaled after the
+ *            rotation so that their kinetic energy is (n_cell - 1) kT
+ *            (two rotated degrees of freedom per particle). */
+typedef enum { NW_SRD_THERMO_NONE = 0, NW_SRD_THERMO_REF_LAB = 1, NW_SRD_THERMO_CELL_REL = 2 } nw_srd_thermostat;
+
+typedef struct NwConfig {
+    uint32_t abi_version;      /* must be NW_ABI_VERSION */
+    int32_t  model;            /* nw_model */
+    int32_t  dim;              /* 2: noise and SRD shift have no z part; 3: full 3D */
+    uint32_t num_filaments;
+    uint32_t filament_size;    /* beads per filament, >= 1 */
+    uint32_t grid[3];          /* bead cell grid */
+    float    cell_size[3];
+    float    origin[3];
+    float    box[3];           /* grid * cell_size */
+    int32_t  boundary[3];      /* nw_boundary per axis */
+    int32_t  hash_mode;        /* nw_hash_mode */
+    float    radius;           /* bead radius (position.w); DEM contact distance 2*radius */
+    float    mass;             /* bead mass (velocity.w) */
+    /* bonded terms */
+    float    bond_k;           /* harmonic bond constant */
+    float    bond_r0;          /* bond rest length */
+    float    bend_k;           /* bending constant of U = k (1 - cos theta) */
+    /* WCA_WORMS pair law */
+    float    lj_epsilon;
+    float    lj_sigma;
+    float    lj_rcut;          /* cut-off; 2^(1/6) sigma gives WCA */
+    int32_t  lj_exclude;       /* same-filament pairs with |i - j| <= lj_exclude are skipped */
+    /* REF_DEM pair law */
+    float    spring;
+    float    damping;
+    float    shear;
+    float    attraction;       /* unused by the reference (commented out) */
+    float    boundary_damping; /* velocity factor of a damped wall */
+    /* activity */
+    float    activity;         /* WCA: tangent drive F_act; REF: extensile amplitude */
+    float    reverse_probability;
+    /* Langevin thermostat */
+    float    gamma;
+    float    kT;
+    int32_t  noise_dt_scaling; /* 1: sigma = sqrt(2 gamma kT / dt); 0: sqrt(2 gamma kT) */
+    int32_t  langevin_with_srd;/* 0: Langevin only when the solvent is off (reference) */
+    float    gravity[3];       /* stored for the API; the reference never applies it */
+    /* SRD solvent */
+    int32_t  srd_enabled;
+    uint32_t num_solvent;
+    uint32_t srd_grid[3];
+    float    srd_cell_size[3];
+    float    srd_alpha;        /* rotation angle, radians */
+    uint32_t srd_gap;          /* collide every srd_gap steps; solvent streams gap*dt */
+    float    srd_kT;
+    float    solvent_mass;
+    float    srd_shift_lo;     /* grid shift drawn in [lo, lo + 1) * srd_cell_size */
+    int32_t  srd_rotate_beads; /* 1: beads are rotated with the solvent; 0: beads only enter the mean */
+    int32_t  srd_thermostat;   /* nw_srd_thermostat */
+    /* run control */
+    uint64_t seed;
+    float    dt;
+    uint32_t reserved[7];
+} NwConfig;
+
+/* Array selectors for nw_get_array / nw_set_array / nw_device_array. */
+typedef enum {
+    NW_POSITION = 0,      /* float4[n_total]  (beads then solvent) */
+    NW_VELOCITY = 1,      /* float4[n_total] */
+    NW_TANGENT = 2,       /* float4[n_beads] */
+    NW_FORCE = 3,         /* float4[n_beads] */
+    NW_FORCE_OLD = 4,     /* float4[n_beads] */
+    NW_HASH = 5,          /* uint[n_beads]   bead cell hash of the last step (unsorted order) */
+    NW_SORTED_INDEX = 6,  /* uint[n_beads]   bead indices in stable cell order */
+    NW_CELL_START = 7,    /* uint[n_cells]   0xffffffff for empty cells */
+    NW_CELL_END = 8,      /* uint[n_cells]   valid where cell start is not empty */
+    NW_SRD_SORTED_INDEX = 9, /* uint[n_total] indices of the last SRD collision, stable cell order */
+    NW_SRD_CELL_START = 10,  /* uint[n_srd_cells] */
+    NW_SRD_CELL_END = 11,    /* uint[n_srd_cells] */
+    NW_SRD_CELL_MEAN = 12    /* float4[n_srd_cells] mass-weighted cell velocity of the last collision */
+} nw_array;
+
+typedef struct nw_system nw_system;
+
+/* ---- configuration ---------------------------------------------------- */
+
+/* Fill *cfg with the defaults of a model.  NW_MODEL_REF_DEM gives the
+ * reference ParticleSystem constructor defaults
+ * (simulation/particleSystem.cpp:39-111, 124-148) for the given grid;
+ * NW_MODEL_WCA_WORMS gives the small 2D worm workload (400 x 10 beads in a
+ * periodic 100 x 100 box, WCA eps = sigma = 1, bond k = 57, r0 = 0.8,
+ * bend k = 10, F_act = 0.5, gamma = 2, kT = 0.1, dt = 0.005). */
+nw_status nw_config_default(NwConfig* cfg, int model, uint32_t num_filaments,
+                            uint32_t filament_size, uint32_t gx, uint32_t gy, uint32_t gz,
+                            int srd);
+
+/* Re-derive box/origin/cell fields after the caller changed grid or cell size
+ * (origin = -box/2 as in simulation/particleSystem.cpp:76-79). */
+nw_status nw_config_finalize(NwConfig* cfg);
+
+/* Check a configuration without creating anything. */
+nw_status nw_config_validate(const NwConfig* cfg);
+
+/* ---- system lifetime ------------------------------------------------------ */
+
+/* Replaces: ParticleSystem::ParticleSystem / _initialize
+ * (simulation/particleSystem.cpp:39-111, 172-223).  Allocates every device
+ * buffer once; nw_step never allocates. */
+nw_status nw_create(const NwConfig* cfg, nw_system** out);
+/* Replaces: ParticleSystem::~ParticleSystem / _finalize
+ * (simulation/particleSystem.cpp:113-117, 225-246); frees everything. */
+nw_status nw_destroy(nw_system* sys);
+
+/* Replaces the ParticleSystem setters + setParameters upload
+ * (simulation/particleSystem.h:53-121, particleSystem_cuda.cu:92-102).
+ * Sizes (filaments, beads, solvent, grids) must not change. */
+nw_status nw_set_config(nw_system* sys, const NwConfig* cfg);
+nw_status nw_get_config(const nw_system* sys, NwConfig* cfg);
+
+/* Counts. */
+nw_status nw_get_counts(const nw_system* sys, uint32_t* n_beads, uint32_t* n_solvent,
+                        uint32_t* n_cells, uint32_t* n_srd_cells);
+
+/* ---- state transfer ------------------------------------------------------- */
+
+/* Replaces: ParticleSystem::setArray (simulation/particleSystem.cpp:561-581).
+ * Copies `count` elements (float4 or uint) from host memory, starting at
+ * element `start`.  Synchronous with respect to the system's stream. */
+nw_status nw_set_array(nw_system* sys, int array, const void* host, uint32_t start, uint32_t count);
+/* Replaces: ParticleSystem::getArray (simulation/particleSystem.cpp:534-559). */
+nw_status nw_get_array(nw_system* sys, int array, void* host, uint32_t start, uint32_t count);
+/* Device pointer of an array (zero-copy access; valid until nw_destroy). */
+nw_status nw_device_array(nw_system* sys, int array, void** dptr);
+/* Zero forces, old forces and the step counter (the reference never zeroes
+ * them: simulation/particleSystem.cpp:202-203). */
+nw_status nw_zero_forces(nw_system* sys);
+
+/* ---- stepping ------------------------------------------------------------- */
+
+/* Replaces: ParticleSystem::update (simulation/particleSystem.cpp:249-339),
+ * nsteps times with step size dt (dt <= 0 uses cfg.dt).  Asynchronous on the
+ * system's stream; runs from a cached CUDA graph when nsteps > 1. */
+nw_status nw_step(nw_system* sys, int nsteps, float dt);
+/* Wait for the stream, then report and clear the device error word. */
+nw_status nw_sync(nw_system* sys);
+nw_status nw_error_word(nw_system* sys, uint32_t* flags);
+nw_status nw_get_step(const nw_system* sys, uint64_t* step);
+nw_status nw_set_step(nw_system* sys, uint64_t step);
+/* Use a caller stream (cudaStream_t passed as void*); NULL restores the
+ * system's own stream. */
+nw_status nw_set_stream(nw_system* sys, void* stream);
+/* Enable or disable CUDA-graph replay for multi-step calls (default on). */
+nw_status nw_set_graphs(nw_system* sys, int enabled);
+/* Run only the SRD sub-step (for tests): shift given in world units. */
+nw_status nw_srd_collide(nw_system* sys, float dt_srd, const float shift[3]);
+
+/* ---- checkpoint / resume -------------------------------------------------- */
+
+/* Bytes needed by nw_checkpoint_save. */
+nw_status nw_checkpoint_size(const nw_system* sys, size_t* bytes);
+/* Binary snapshot: config, step counter, positions, velocities, forces,
+ * old forces, tangents.  Resuming from it is bit-exact. */
+nw_status nw_checkpoint_save(nw_system* sys, void* host_buf, size_t bytes);
+nw_status nw_checkpoint_load(nw_system* sys, const void* host_buf, size_t bytes);
+
+/* ---- misc ----------------------------------------------------------------- */
+
+const char* nw_status_string(nw_status s);
+uint32_t nw_abi_version(void);
+/* sizeof(NwConfig) as compiled into the library (binding layout check). */
+size_t nw_config_size(void);
+/* Number of kernels the last nw_step call launched (graph replays count the
+ * kernels inside the graph). */
+nw_status nw_last_launch_count(const nw_system* sys, uint64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NWGB_H */

@@ -1,0 +1,620 @@
+// nw_engine.cu — the handle API of include/nwgb.h: system lifetime, state
+// transfer, the step launcher with CUDA-graph replay, SRD, checkpoints.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "nw_engine.h"
+
+namespace nw {
+
+DevParams make_dev_params(const NwConfig& c, float dt)
+{
+    DevParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.model = c.model;
+    P.dim = c.dim;
+    P.hash_mode = c.hash_mode;
+    P.nf = c.num_filaments;
+    P.L = c.filament_size;
+    P.nb = c.num_filaments * c.filament_size;
+    P.ns = c.srd_enabled ? c.num_solvent : 0u;
+    P.ntotal = P.nb + P.ns;
+    P.ncells = 1;
+    for (int a = 0; a < 3; ++a) {
+        P.grid[a] = c.grid[a];
+        P.ncells *= c.grid[a];
+        P.cell[a] = c.cell_size[a];
+        P.origin[a] = c.origin[a];
+        P.box[a] = c.box[a];
+        P.bnd[a] = c.boundary[a];
+        P.srd_grid[a] = c.srd_grid[a] ? c.srd_grid[a] : 1u;
+        P.srd_cell[a] = c.srd_cell_size[a];
+    }
+    P.srd_ncells = P.srd_grid[0] * P.srd_grid[1] * P.srd_grid[2];
+    P.radius = c.radius;
+    P.mass = c.mass;
+    P.bond_k = c.bond_k;
+    P.bond_r0 = c.bond_r0;
+    P.bend_k = c.bend_k;
+    const float s6 = powf(c.lj_sigma, 6.0f);
+    P.lj_amp = 24.0f * c.lj_epsilon * s6;
+    P.lj_two_s6 = 2.0f * s6;
+    P.lj_rc2 = c.lj_rcut * c.lj_rcut;
+    P.lj_exclude = c.lj_exclude;
+    P.spring = c.spring;
+    P.damping = c.damping;
+    P.shear = c.shear;
+    P.bdamp = c.boundary_damping;
+    P.activity = c.activity;
+    P.reverse_p = c.reverse_probability;
+    P.reverse_on = c.reverse_probability > 0.0f;
+    P.gamma = c.gamma;
+    float s2 = 2.0f * c.gamma * c.kT;
+    if (c.noise_dt_scaling) s2 = s2 / dt;
+    P.noise_sigma = sqrtf(s2);
+    P.langevin_on = (!c.srd_enabled || c.langevin_with_srd) ? 1 : 0;
+    P.srd_on = c.srd_enabled;
+    P.srd_alpha = c.srd_alpha;
+    P.srd_kT = c.srd_kT;
+    P.srd_shift_lo = c.srd_shift_lo;
+    P.srd_rotate_beads = c.srd_rotate_beads;
+    P.srd_thermo = c.srd_thermostat;
+    P.seed_lo = (uint32_t)c.seed;
+    P.seed_hi = (uint32_t)(c.seed >> 32);
+    return P;
+}
+
+static uint32_t cdiv(uint64_t a, uint32_t b) { return (uint32_t)((a + b - 1) / b); }
+
+// Filaments per block of the filament pass: whole filaments, about 256 threads.
+static uint32_t filaments_per_block(uint32_t L, uint32_t nf)
+{
+    uint32_t fpb = L >= 256 ? 1u : 256u / L;
+    if (fpb > nf && nf > 0) fpb = nf;
+    return fpb ? fpb : 1u;
+}
+
+uint64_t enqueue_bead_step(const DevParams& P, const StepBuffers& B, uint32_t nchunks, uint32_t step_off, float dt,
+                           cudaStream_t s)
+{
+    if (P.nb == 0) return 0;
+    const uint32_t fpb = filaments_per_block(P.L, P.nf);
+    const uint32_t beads = fpb * P.L;
+    const uint32_t threads = (beads + 31u) & ~31u;
+    const size_t smem = (size_t)beads * sizeof(float4) * (P.reverse_on ? 3u : 1u);
+    filament_pass_kernel<<<cdiv(P.nf, fpb), threads, smem, s>>>(P, B, step_off, dt, fpb);
+    scan_cells_kernel<true><<<nchunks, 512, 0, s>>>(B.cell_count, B.chunk_count, P.ncells, B.cell_offset, B.cell_start,
+                                                    B.cell_end);
+    scatter_kernel<<<cdiv(P.nb, 256), 256, 0, s>>>(B.hash, B.slot, B.cell_offset, B.tmp_index, P.nb, B.chunk_count,
+                                                   nchunks);
+    if (P.model == NW_MODEL_REF_DEM) {
+        stable_gather_kernel<true><<<cdiv(P.nb, 256), 256, 0, s>>>(P, B);
+        pair_ref_kernel<<<cdiv(P.nb, 256), 256, 0, s>>>(P, B);
+    } else {
+        stable_gather_kernel<false><<<cdiv(P.nb, 256), 256, 0, s>>>(P, B);
+        pair_wca_kernel<<<cdiv(P.nb, 256), 256, 0, s>>>(P, B);
+    }
+    return 5;
+}
+
+uint64_t enqueue_srd(const DevParams& P, const StepBuffers& B, uint32_t srd_nchunks, uint32_t step_off, float dt_srd,
+                     int shift_from_step, float3 shift, cudaStream_t s)
+{
+    if (P.ntotal == 0) return 0;
+    srd_hash_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(P, B, step_off, shift_from_step, shift);
+    scan_cells_kernel<true><<<srd_nchunks, 512, 0, s>>>(B.srd_count, B.srd_chunk, P.srd_ncells, B.srd_offset,
+                                                        B.srd_start, B.srd_end);
+    scatter_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(B.srd_hash, B.srd_slot, B.srd_offset, B.srd_tmp, P.ntotal,
+                                                       B.srd_chunk, srd_nchunks);
+    srd_collide_kernel<<<cdiv(P.srd_ncells, 256), 256, 0, s>>>(P, B, step_off, dt_srd);
+    return 4;
+}
+
+}  // namespace nw
+
+using namespace nw;
+
+struct GraphEntry {
+    int nsteps;
+    uint32_t dt_bits;
+    uint32_t phase;
+    uint64_t version;
+    cudaGraphExec_t exec;
+    uint64_t launches;
+};
+
+struct nw_system {
+    NwConfig cfg;
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    StepBuffers B;
+    uint32_t nb = 0, ns = 0, ntotal = 0, ncells = 0, nchunks = 0, srd_ncells = 0, srd_nchunks = 0;
+    uint64_t step = 0;
+    uint64_t version = 1;
+    bool use_graphs = true;
+    std::vector<GraphEntry> graphs;
+    uint64_t last_launches = 0;
+    std::vector<void*> allocs;
+};
+
+namespace {
+
+nw_status alloc(nw_system* s, void** p, size_t bytes)
+{
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    if (cudaMalloc(p, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return NW_ERR_NOMEM;
+    }
+    s->allocs.push_back(*p);
+    return NW_OK;
+}
+
+template <class T>
+nw_status alloc_n(nw_system* s, T** p, size_t n)
+{
+    return alloc(s, reinterpret_cast<void**>(p), n * sizeof(T));
+}
+
+void free_all(nw_system* s)
+{
+    for (auto& g : s->graphs) cudaGraphExecDestroy(g.exec);
+    s->graphs.clear();
+    for (void* p : s->allocs) cudaFree(p);
+    s->allocs.clear();
+    if (s->own_stream) cudaStreamDestroy(s->own_stream);
+    s->own_stream = nullptr;
+}
+
+void drop_graphs(nw_system* s)
+{
+    for (auto& g : s->graphs) cudaGraphExecDestroy(g.exec);
+    s->graphs.clear();
+    s->version++;
+}
+
+struct ArrayInfo {
+    void* ptr;
+    size_t elem;
+    size_t count;
+};
+
+ArrayInfo array_info(nw_system* s, int array)
+{
+    const StepBuffers& B = s->B;
+    switch (array) {
+    case NW_POSITION: return {B.pos, sizeof(float4), s->ntotal};
+    case NW_VELOCITY: return {B.vel, sizeof(float4), s->ntotal};
+    case NW_TANGENT: return {B.tangent, sizeof(float4), s->nb};
+    case NW_FORCE: return {B.force, sizeof(float4), s->nb};
+    case NW_FORCE_OLD: return {B.force_old, sizeof(float4), s->nb};
+    case NW_HASH: return {B.hash, sizeof(uint32_t), s->nb};
+    case NW_SORTED_INDEX: return {B.sorted_index, sizeof(uint32_t), s->nb};
+    case NW_CELL_START: return {B.cell_start, sizeof(uint32_t), s->ncells};
+    case NW_CELL_END: return {B.cell_end, sizeof(uint32_t), s->ncells};
+    case NW_SRD_SORTED_INDEX: return {B.srd_sorted_index, sizeof(uint32_t), s->cfg.srd_enabled ? s->ntotal : 0u};
+    case NW_SRD_CELL_START: return {B.srd_start, sizeof(uint32_t), s->cfg.srd_enabled ? s->srd_ncells : 0u};
+    case NW_SRD_CELL_END: return {B.srd_end, sizeof(uint32_t), s->cfg.srd_enabled ? s->srd_ncells : 0u};
+    case NW_SRD_CELL_MEAN: return {B.srd_mean, sizeof(float4), s->cfg.srd_enabled ? s->srd_ncells : 0u};
+    default: return {nullptr, 0, 0};
+    }
+}
+
+// Enqueue `nsteps` steps starting at device step base + 0 and advance the base.
+uint64_t enqueue_steps(nw_system* s, int nsteps, float dt, uint64_t first_step)
+{
+    const DevParams P = make_dev_params(s->cfg, dt);
+    uint64_t launches = 0;
+    for (int j = 0; j < nsteps; ++j) {
+        launches += enqueue_bead_step(P, s->B, s->nchunks, (uint32_t)j, dt, s->stream);
+        const uint64_t st = first_step + (uint64_t)j;
+        if (s->cfg.srd_enabled && (st % s->cfg.srd_gap) == 0)
+            launches += enqueue_srd(P, s->B, s->srd_nchunks, (uint32_t)j, dt * (float)s->cfg.srd_gap, 1,
+                                    make_float3(0.f, 0.f, 0.f), s->stream);
+    }
+    advance_step_kernel<<<1, 1, 0, s->stream>>>(s->B.step_base, (unsigned long long)nsteps);
+    return launches + 1;
+}
+
+nw_status cuda_status(cudaError_t e)
+{
+    if (e == cudaSuccess) return NW_OK;
+    if (e == cudaErrorMemoryAllocation) return NW_ERR_NOMEM;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return NW_ERR_NO_DEVICE;
+    std::fprintf(stderr, "[nwgb] CUDA error: %s\n", cudaGetErrorString(e));
+    return NW_ERR_CUDA;
+}
+
+}  // namespace
+
+extern "C" {
+
+nw_status nw_create(const NwConfig* cfg, nw_system** out)
+{
+    if (!out) return NW_ERR_INVALID;
+    *out = nullptr;
+    nw_status st = nw_config_validate(cfg);
+    if (st != NW_OK) return st;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return NW_ERR_NO_DEVICE;
+    }
+    nw_system* s = new nw_system();
+    s->cfg = *cfg;
+    cudaGetDevice(&s->device);
+    if (cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete s;
+        return NW_ERR_CUDA;
+    }
+    s->stream = s->own_stream;
+    s->nb = cfg->num_filaments * cfg->filament_size;
+    s->ns = cfg->srd_enabled ? cfg->num_solvent : 0u;
+    s->ntotal = s->nb + s->ns;
+    s->ncells = cfg->grid[0] * cfg->grid[1] * cfg->grid[2];
+    s->nchunks = (s->ncells + kChunk - 1) / kChunk;
+    s->srd_ncells = cfg->srd_enabled ? cfg->srd_grid[0] * cfg->srd_grid[1] * cfg->srd_grid[2] : 0u;
+    s->srd_nchunks = (s->srd_ncells + kChunk - 1) / kChunk;
+    StepBuffers& B = s->B;
+    std::memset(&B, 0, sizeof(B));
+    const size_t nb = s->nb, nt = s->ntotal, C = s->ncells;
+    const bool ref = cfg->model == NW_MODEL_REF_DEM;
+    st = NW_OK;
+    auto A = [&](nw_status x) {
+        if (st == NW_OK) st = x;
+    };
+    A(alloc_n(s, &B.pos, nt));
+    A(alloc_n(s, &B.vel, nt));
+    A(alloc_n(s, &B.force, nb));
+    A(alloc_n(s, &B.force_old, nb));
+    A(alloc_n(s, &B.tangent, nb));
+    A(alloc_n(s, &B.hash, nb));
+    A(alloc_n(s, &B.slot, nb));
+    A(alloc_n(s, &B.tmp_index, nb));
+    A(alloc_n(s, &B.sorted_index, nb));
+    A(alloc_n(s, &B.sorted_hash, nb));
+    A(alloc_n(s, &B.cell_count, C + 8));
+    A(alloc_n(s, &B.cell_offset, C + 8));
+    A(alloc_n(s, &B.cell_start, C + 8));
+    A(alloc_n(s, &B.cell_end, C + 8));
+    A(alloc_n(s, &B.chunk_count, (size_t)s->nchunks + 1));
+    A(alloc_n(s, &B.sorted_pos, nb));
+    if (ref) {
+        A(alloc_n(s, &B.sorted_vel, nb));
+        A(alloc_n(s, &B.sorted_tan, nb));
+    }
+    if (cfg->srd_enabled) {
+        const size_t Cs = s->srd_ncells;
+        A(alloc_n(s, &B.srd_hash, nt));
+        A(alloc_n(s, &B.srd_slot, nt));
+        A(alloc_n(s, &B.srd_tmp, nt));
+        A(alloc_n(s, &B.srd_sorted_index, nt));
+        A(alloc_n(s, &B.srd_count, Cs + 8));
+        A(alloc_n(s, &B.srd_offset, Cs + 8));
+        A(alloc_n(s, &B.srd_start, Cs + 8));
+        A(alloc_n(s, &B.srd_end, Cs + 8));
+        A(alloc_n(s, &B.srd_chunk, (size_t)s->srd_nchunks + 1));
+        A(alloc_n(s, &B.srd_mean, Cs));
+    }
+    A(alloc_n(s, &B.err, 4));
+    A(alloc_n(s, &B.step_base, 1));
+    if (st != NW_OK) {
+        free_all(s);
+        delete s;
+        return st;
+    }
+    // counters must start at zero; state starts empty
+    cudaError_t e = cudaSuccess;
+    auto Z = [&](void* p, size_t bytes) {
+        if (p && e == cudaSuccess) e = cudaMemsetAsync(p, 0, bytes, s->stream);
+    };
+    Z(B.pos, nt * 16);
+    Z(B.vel, nt * 16);
+    Z(B.force, nb * 16);
+    Z(B.force_old, nb * 16);
+    Z(B.tangent, nb * 16);
+    Z(B.cell_count, (C + 8) * 4);
+    Z(B.chunk_count, ((size_t)s->nchunks + 1) * 4);
+    if (cfg->srd_enabled) {
+        Z(B.srd_count, ((size_t)s->srd_ncells + 8) * 4);
+        Z(B.srd_chunk, ((size_t)s->srd_nchunks + 1) * 4);
+        Z(B.srd_mean, (size_t)s->srd_ncells * 16);
+    }
+    Z(B.err, 16);
+    Z(B.step_base, 8);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.cell_start, 0xff, (C + 8) * 4, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.cell_end, 0xff, (C + 8) * 4, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) {
+        st = cuda_status(e);
+        free_all(s);
+        delete s;
+        return st;
+    }
+    *out = s;
+    return NW_OK;
+}
+
+nw_status nw_destroy(nw_system* s)
+{
+    if (!s) return NW_ERR_INVALID;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    free_all(s);
+    delete s;
+    return NW_OK;
+}
+
+nw_status nw_set_config(nw_system* s, const NwConfig* cfg)
+{
+    if (!s || !cfg) return NW_ERR_INVALID;
+    nw_status st = nw_config_validate(cfg);
+    if (st != NW_OK) return st;
+    const NwConfig& o = s->cfg;
+    if (cfg->model != o.model || cfg->num_filaments != o.num_filaments || cfg->filament_size != o.filament_size ||
+        cfg->srd_enabled != o.srd_enabled || (cfg->srd_enabled && cfg->num_solvent != o.num_solvent))
+        return NW_ERR_INVALID;
+    for (int a = 0; a < 3; ++a)
+        if (cfg->grid[a] != o.grid[a] || (cfg->srd_enabled && cfg->srd_grid[a] != o.srd_grid[a]))
+            return NW_ERR_INVALID;
+    s->cfg = *cfg;
+    drop_graphs(s);
+    return NW_OK;
+}
+
+nw_status nw_get_config(const nw_system* s, NwConfig* cfg)
+{
+    if (!s || !cfg) return NW_ERR_INVALID;
+    *cfg = s->cfg;
+    return NW_OK;
+}
+
+nw_status nw_get_counts(const nw_system* s, uint32_t* nb, uint32_t* ns, uint32_t* nc, uint32_t* nsc)
+{
+    if (!s) return NW_ERR_INVALID;
+    if (nb) *nb = s->nb;
+    if (ns) *ns = s->ns;
+    if (nc) *nc = s->ncells;
+    if (nsc) *nsc = s->srd_ncells;
+    return NW_OK;
+}
+
+nw_status nw_set_array(nw_system* s, int array, const void* host, uint32_t start, uint32_t count)
+{
+    if (!s || (!host && count)) return NW_ERR_INVALID;
+    ArrayInfo a = array_info(s, array);
+    if (!a.ptr || (uint64_t)start + count > a.count) return NW_ERR_INVALID;
+    if (!count) return NW_OK;
+    cudaError_t e = cudaMemcpyAsync((char*)a.ptr + (size_t)start * a.elem, host, (size_t)count * a.elem,
+                                    cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    return cuda_status(e);
+}
+
+nw_status nw_get_array(nw_system* s, int array, void* host, uint32_t start, uint32_t count)
+{
+    if (!s || (!host && count)) return NW_ERR_INVALID;
+    ArrayInfo a = array_info(s, array);
+    if (!a.ptr || (uint64_t)start + count > a.count) return NW_ERR_INVALID;
+    if (!count) return NW_OK;
+    cudaError_t e = cudaMemcpyAsync(host, (const char*)a.ptr + (size_t)start * a.elem, (size_t)count * a.elem,
+                                    cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    return cuda_status(e);
+}
+
+nw_status nw_device_array(nw_system* s, int array, void** dptr)
+{
+    if (!s || !dptr) return NW_ERR_INVALID;
+    ArrayInfo a = array_info(s, array);
+    if (!a.ptr) return NW_ERR_INVALID;
+    *dptr = a.ptr;
+    return NW_OK;
+}
+
+nw_status nw_zero_forces(nw_system* s)
+{
+    if (!s) return NW_ERR_INVALID;
+    cudaError_t e = cudaMemsetAsync(s->B.force, 0, (size_t)s->nb * 16, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->B.force_old, 0, (size_t)s->nb * 16, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    return cuda_status(e);
+}
+
+nw_status nw_step(nw_system* s, int nsteps, float dt)
+{
+    if (!s || nsteps < 0) return NW_ERR_INVALID;
+    if (nsteps == 0) return NW_OK;
+    if (!(dt > 0.0f)) dt = s->cfg.dt;
+    if (!std::isfinite(dt)) return NW_ERR_INVALID;
+    const uint32_t phase = s->cfg.srd_enabled ? (uint32_t)(s->step % s->cfg.srd_gap) : 0u;
+    cudaError_t e = cudaSuccess;
+    if (s->use_graphs && nsteps > 1) {
+        uint32_t bits;
+        std::memcpy(&bits, &dt, 4);
+        GraphEntry* hit = nullptr;
+        for (auto& g : s->graphs)
+            if (g.nsteps == nsteps && g.dt_bits == bits && g.phase == phase && g.version == s->version) hit = &g;
+        if (!hit) {
+            if (s->graphs.size() >= 8) drop_graphs(s);
+            cudaGraph_t graph = nullptr;
+            e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) return cuda_status(e);
+            uint64_t launches = enqueue_steps(s, nsteps, dt, s->step);
+            e = cudaStreamEndCapture(s->stream, &graph);
+            if (e != cudaSuccess) return cuda_status(e);
+            cudaGraphExec_t exec = nullptr;
+            e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return cuda_status(e);
+            s->graphs.push_back({nsteps, bits, phase, s->version, exec, launches});
+            hit = &s->graphs.back();
+        }
+        e = cudaGraphLaunch(hit->exec, s->stream);
+        s->last_launches = hit->launches;
+    } else {
+        s->last_launches = enqueue_steps(s, nsteps, dt, s->step);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) return cuda_status(e);
+    s->step += (uint64_t)nsteps;
+    return NW_OK;
+}
+
+nw_status nw_error_word(nw_system* s, uint32_t* flags)
+{
+    if (!s) return NW_ERR_INVALID;
+    uint32_t f = 0;
+    cudaError_t e = cudaMemcpyAsync(&f, s->B.err, 4, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->B.err, 0, 4, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (flags) *flags = f;
+    return cuda_status(e);
+}
+
+nw_status nw_sync(nw_system* s)
+{
+    if (!s) return NW_ERR_INVALID;
+    uint32_t f = 0;
+    nw_status st = nw_error_word(s, &f);
+    if (st != NW_OK) return st;
+    if (f & NW_EFLAG_NONFINITE) return NW_ERR_NONFINITE;
+    if (f & NW_EFLAG_CELL_OVERFLOW) return NW_ERR_CELL_OVERFLOW;
+    if (f & NW_EFLAG_TIMEOUT) return NW_ERR_TIMEOUT;
+    if (f & NW_EFLAG_BAD_INDEX) return NW_ERR_INVALID;
+    return NW_OK;
+}
+
+nw_status nw_get_step(const nw_system* s, uint64_t* step)
+{
+    if (!s || !step) return NW_ERR_INVALID;
+    *step = s->step;
+    return NW_OK;
+}
+
+nw_status nw_set_step(nw_system* s, uint64_t step)
+{
+    if (!s) return NW_ERR_INVALID;
+    unsigned long long v = step;
+    cudaError_t e = cudaMemcpyAsync(s->B.step_base, &v, 8, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) s->step = step;
+    return cuda_status(e);
+}
+
+nw_status nw_set_stream(nw_system* s, void* stream)
+{
+    if (!s) return NW_ERR_INVALID;
+    cudaStreamSynchronize(s->stream);
+    s->stream = stream ? (cudaStream_t)stream : s->own_stream;
+    drop_graphs(s);
+    return NW_OK;
+}
+
+nw_status nw_set_graphs(nw_system* s, int enabled)
+{
+    if (!s) return NW_ERR_INVALID;
+    s->use_graphs = enabled != 0;
+    return NW_OK;
+}
+
+nw_status nw_srd_collide(nw_system* s, float dt_srd, const float shift[3])
+{
+    if (!s || !shift) return NW_ERR_INVALID;
+    if (!s->cfg.srd_enabled) return NW_ERR_UNSUPPORTED;
+    const DevParams P = make_dev_params(s->cfg, s->cfg.dt);
+    s->last_launches = enqueue_srd(P, s->B, s->srd_nchunks, 0u, dt_srd, 0, make_float3(shift[0], shift[1], shift[2]),
+                                   s->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    return cuda_status(e);
+}
+
+// ---- checkpoints ---------------------------------------------------------------
+
+struct CkptHeader {
+    char magic[8];
+    uint32_t version, cfg_bytes, nb, ntotal;
+    uint64_t step;
+};
+
+nw_status nw_checkpoint_size(const nw_system* s, size_t* bytes)
+{
+    if (!s || !bytes) return NW_ERR_INVALID;
+    *bytes = sizeof(CkptHeader) + sizeof(NwConfig) + (size_t)s->ntotal * 32 + (size_t)s->nb * 48;
+    return NW_OK;
+}
+
+nw_status nw_checkpoint_save(nw_system* s, void* buf, size_t bytes)
+{
+    size_t need = 0;
+    if (nw_checkpoint_size(s, &need) != NW_OK || !buf || bytes < need) return NW_ERR_INVALID;
+    char* p = (char*)buf;
+    CkptHeader h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, "NWGBCKP", 8);
+    h.version = 1;
+    h.cfg_bytes = sizeof(NwConfig);
+    h.nb = s->nb;
+    h.ntotal = s->ntotal;
+    h.step = s->step;
+    std::memcpy(p, &h, sizeof(h));
+    p += sizeof(h);
+    std::memcpy(p, &s->cfg, sizeof(NwConfig));
+    p += sizeof(NwConfig);
+    struct {
+        void* d;
+        size_t n;
+    } parts[] = {{s->B.pos, (size_t)s->ntotal * 16}, {s->B.vel, (size_t)s->ntotal * 16}, {s->B.force, (size_t)s->nb * 16},
+                 {s->B.force_old, (size_t)s->nb * 16}, {s->B.tangent, (size_t)s->nb * 16}};
+    cudaError_t e = cudaSuccess;
+    for (auto& q : parts) {
+        if (q.n && e == cudaSuccess) e = cudaMemcpyAsync(p, q.d, q.n, cudaMemcpyDeviceToHost, s->stream);
+        p += q.n;
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    return cuda_status(e);
+}
+
+nw_status nw_checkpoint_load(nw_system* s, const void* buf, size_t bytes)
+{
+    size_t need = 0;
+    if (nw_checkpoint_size(s, &need) != NW_OK || !buf || bytes < need) return NW_ERR_INVALID;
+    const char* p = (const char*)buf;
+    CkptHeader h;
+    std::memcpy(&h, p, sizeof(h));
+    if (std::memcmp(h.magic, "NWGBCKP", 8) != 0 || h.version != 1 || h.cfg_bytes != sizeof(NwConfig) ||
+        h.nb != s->nb || h.ntotal != s->ntotal)
+        return NW_ERR_INVALID;
+    p += sizeof(h);
+    NwConfig cfg;
+    std::memcpy(&cfg, p, sizeof(cfg));
+    p += sizeof(NwConfig);
+    nw_status st = nw_set_config(s, &cfg);
+    if (st != NW_OK) return st;
+    struct {
+        void* d;
+        size_t n;
+    } parts[] = {{s->B.pos, (size_t)s->ntotal * 16}, {s->B.vel, (size_t)s->ntotal * 16}, {s->B.force, (size_t)s->nb * 16},
+                 {s->B.force_old, (size_t)s->nb * 16}, {s->B.tangent, (size_t)s->nb * 16}};
+    cudaError_t e = cudaSuccess;
+    for (auto& q : parts) {
+        if (q.n && e == cudaSuccess) e = cudaMemcpyAsync(q.d, p, q.n, cudaMemcpyHostToDevice, s->stream);
+        p += q.n;
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return cuda_status(e);
+    return nw_set_step(s, h.step);
+}
+
+nw_status nw_last_launch_count(const nw_system* s, uint64_t* launches)
+{
+    if (!s || !launches) return NW_ERR_INVALID;
+    *launches = s->last_launches;
+    return NW_OK;
+}
+
+}  // extern "C"

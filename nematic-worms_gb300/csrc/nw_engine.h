@@ -1,0 +1,21 @@
+// nw_engine.h — host-side launch helpers shared by the handle API, the
+// batched engine and the legacy C-ABI layer.
+#pragma once
+
+#include "nw_kernels.cuh"
+
+namespace nw {
+
+// Kernel parameter block for a configuration and step size.
+DevParams make_dev_params(const NwConfig& c, float dt);
+
+// Enqueue one bead step (5 kernels); returns the number of launches.
+uint64_t enqueue_bead_step(const DevParams& P, const StepBuffers& B, uint32_t nchunks, uint32_t step_off, float dt,
+                           cudaStream_t s);
+
+// Enqueue one SRD collision (4 kernels).  With shift_from_step the grid
+// shift is drawn on the device from (seed, step); otherwise `shift` is used.
+uint64_t enqueue_srd(const DevParams& P, const StepBuffers& B, uint32_t srd_nchunks, uint32_t step_off, float dt_srd,
+                     int shift_from_step, float3 shift, cudaStream_t s);
+
+}  // namespace nw

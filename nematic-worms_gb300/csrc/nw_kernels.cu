@@ -1,0 +1,327 @@
+// nw_kernels.cu — definitions of the non-template step kernels declared in
+// nw_kernels.cuh (one translation unit owns each kernel).
+#include "nw_kernels.cuh"
+
+namespace nw {
+
+__global__ void __launch_bounds__(1024) filament_pass_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
+                                                             float dt, uint32_t fpb)
+{
+    extern __shared__ float4 sm[];
+    const uint32_t L = P.L;
+    const uint32_t beads = fpb * L;
+    const uint32_t t = threadIdx.x;
+    const uint32_t w0 = blockIdx.x * fpb;
+    const uint32_t i = w0 * L + t;
+    const bool active = t < beads && i < P.nb;
+    const unsigned long long step = *S.step_base + step_off;
+
+    float4 nP = make_float4(0.f, 0.f, 0.f, 0.f), nV = nP, nFo = nP;
+    if (active) {
+        const float4 P4 = S.pos[i], V4 = S.vel[i], F4 = S.force[i], Fo4 = S.force_old[i];
+        float3 p = f3(P4), v = f3(V4);
+        const float3 f = f3(F4), fo = f3(Fo4);
+        // velocity Verlet (particles_kernel_impl.cuh:93-97)
+        const float3 dv = (0.5f * (f + fo)) * dt;
+        v += dv;
+        const float3 dr = v * dt + ((0.5f * f) * dt) * dt;
+        p += dr;
+        apply_boundaries(P, p, v, dr, P.radius);
+        nP = make_float4(p.x, p.y, p.z, P4.w);
+        nV = make_float4(v.x, v.y, v.z, V4.w);
+        nFo = make_float4(f.x, f.y, f.z, Fo4.w);
+    }
+    if (P.reverse_on) {
+        // reverseFilamentsKernel (particles_kernel_impl.cuh:820-857)
+        if (active) {
+            sm[t] = nP;
+            sm[beads + t] = nV;
+            sm[2 * beads + t] = nFo;
+        }
+        __syncthreads();
+        if (active) {
+            const uint32_t wl = t / L, c = t - wl * L;
+            const float u = u01(rng_draw(P, w0 + wl, step, kRngReverse).x);
+            if (u <= P.reverse_p) {
+                const uint32_t src = wl * L + (L - 1u - c);
+                nP = sm[src];
+                nV = sm[beads + src];
+                nFo = sm[2 * beads + src];
+            }
+        }
+        __syncthreads();
+    }
+    if (active) sm[t] = nP;
+    __syncthreads();
+    if (!active) return;
+
+    const uint32_t wl = t / L, c = t - wl * L;
+    const float4* R = sm + wl * L;
+    float3 fs = zero3();
+    if (P.langevin_on) {
+        // langevinKernel (particles_kernel_impl.cuh:859-874), Philox noise in registers
+        const float4 z = normal4(rng_draw(P, i, step, kRngLangevin));
+        const float3 g = make_float3(P.noise_sigma * z.x, P.noise_sigma * z.y, P.dim >= 3 ? P.noise_sigma * z.z : 0.f);
+        float3 fl = zero3() - P.gamma * f3(nV);
+        fl += g;
+        fs = fl;
+    }
+    // bending contributions in the reference's triple order p = c-2, c-1, c
+    if (L >= 3) {
+        if (c >= 2) fs += bend_triple(P, f3(R[c - 2]), f3(R[c - 1]), f3(R[c])).fk;
+        if (c >= 1 && c + 1 < L) fs += bend_triple(P, f3(R[c - 1]), f3(R[c]), f3(R[c + 1])).fj;
+        if (c + 2 < L) fs += bend_triple(P, f3(R[c]), f3(R[c + 1]), f3(R[c + 2])).fi;
+    }
+    bool wt = false;
+    float3 tg = zero3();
+    if (L >= 3) {
+        if (c == 0) {
+            tg = tangent_of(P, f3(R[0]), f3(R[1]));
+            wt = true;
+        } else if (c == L - 1) {
+            if (L > 3) {
+                tg = tangent_of(P, f3(R[L - 2]), f3(R[L - 1]));
+                wt = true;
+            }
+        } else {
+            tg = tangent_of(P, f3(R[c - 1]), f3(R[c + 1]));
+            wt = true;
+        }
+    }
+    if (P.model == NW_MODEL_WCA_WORMS) {
+        const float3 me = f3(R[c]);
+        if (c + 1 < L) wca_bond(P, me, f3(R[c + 1]), fs);
+        if (c > 0) wca_bond(P, me, f3(R[c - 1]), fs);
+        if (c + 1 < L) wca_drive(P, me, f3(R[c + 1]), fs);
+    }
+    S.pos[i] = nP;
+    S.vel[i] = nV;
+    S.force_old[i] = nFo;
+    S.force[i] = make_float4(fs.x, fs.y, fs.z, 0.f);
+    if (wt) S.tangent[i] = make_float4(tg.x, tg.y, tg.z, 0.f);
+    if (!finite3(f3(nP)) || !finite3(fs)) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
+
+    const uint32_t h = bead_hash(P, f3(nP));
+    S.hash[i] = h;
+    S.slot[i] = count_into_cell(S.cell_count, S.chunk_count, h);
+}
+
+__global__ void __launch_bounds__(256) scatter_kernel(const uint32_t* __restrict__ hash,
+                                                      const uint32_t* __restrict__ slot,
+                                                      const uint32_t* __restrict__ offset, uint32_t* __restrict__ tmp,
+                                                      uint32_t n, uint32_t* __restrict__ chunk_count, uint32_t nchunks)
+{
+    if (blockIdx.x == 0)
+        for (uint32_t k = threadIdx.x; k < nchunks; k += blockDim.x) chunk_count[k] = 0u;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) tmp[offset[hash[i]] + slot[i]] = i;
+}
+
+__global__ void __launch_bounds__(256) pair_ref_kernel(const DevParams P, const StepBuffers S)
+{
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.nb) return;
+    const float3 r = f3(S.sorted_pos[p]);
+    const float3 v = f3(S.sorted_vel[p]);
+    const float3 t = f3(S.sorted_tan[p]);
+    const int3 g = grid_pos(P, r);
+    const uint32_t me = S.sorted_index[p];
+    const uint32_t fI = me / P.L, cI = me - fI * P.L;
+    float3 total = zero3();
+    if (P.grid[2] == 1u) {
+        float3 cs[9];
+#pragma unroll
+        for (int y = -1; y <= 1; ++y)
+#pragma unroll
+            for (int x = -1; x <= 1; ++x) {
+                const uint32_t h = cell_hash(P, cell_coord(P, 0, g.x + x), cell_coord(P, 1, g.y + y), cell_coord(P, 2, g.z));
+                cs[(y + 1) * 3 + (x + 1)] = ref_cell_sum(P, S, h, p, r, v, t, fI, cI);
+            }
+#pragma unroll
+        for (int z = 0; z < 3; ++z)
+#pragma unroll
+            for (int k = 0; k < 9; ++k) total += cs[k];
+    } else {
+        for (int z = -1; z <= 1; ++z)
+            for (int y = -1; y <= 1; ++y)
+                for (int x = -1; x <= 1; ++x) {
+                    const uint32_t h =
+                        cell_hash(P, cell_coord(P, 0, g.x + x), cell_coord(P, 1, g.y + y), cell_coord(P, 2, g.z + z));
+                    total += ref_cell_sum(P, S, h, p, r, v, t, fI, cI);
+                }
+    }
+    float4 F = S.force[me];
+    F.x += total.x;
+    F.y += total.y;
+    F.z += total.z;
+    S.force[me] = F;
+    if (!finite3(f3(F))) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
+}
+
+__global__ void __launch_bounds__(256) pair_wca_kernel(const DevParams P, const StepBuffers S)
+{
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.nb) return;
+    const float3 r = f3(S.sorted_pos[p]);
+    const int3 g = grid_pos(P, r);
+    uint32_t cx[3], cy[3], cz[3];
+    const int nx = axis_cells(P, 0, cell_coord(P, 0, g.x), cx);
+    const int ny = axis_cells(P, 1, cell_coord(P, 1, g.y), cy);
+    const int nz = axis_cells(P, 2, cell_coord(P, 2, g.z), cz);
+    const uint32_t me = S.sorted_index[p];
+    const uint32_t fI = me / P.L;
+    const int cI = (int)(me - fI * P.L);
+    float3 f = zero3();
+    for (int kz = 0; kz < nz; ++kz)
+        for (int ky = 0; ky < ny; ++ky)
+            for (int kx = 0; kx < nx; ++kx) {
+                const uint32_t h = (cz[kz] * P.grid[1] + cy[ky]) * P.grid[0] + cx[kx];
+                const uint32_t s0 = __ldg(&S.cell_start[h]);
+                if (s0 == kEmpty) continue;
+                uint32_t s1 = __ldg(&S.cell_end[h]);
+                if (s1 - s0 > kPairCap) {
+                    atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
+                    s1 = s0 + kPairCap;
+                }
+                for (uint32_t j = s0; j < s1; ++j) {
+                    if (j == p) continue;
+                    const uint32_t o = __ldg(&S.sorted_index[j]);
+                    const uint32_t fJ = o / P.L;
+                    if (fJ == fI) {
+                        const int d = (int)(o - fJ * P.L) - cI;
+                        if (d <= P.lj_exclude && d >= -P.lj_exclude) continue;
+                    }
+                    float3 dr = f3(__ldg(&S.sorted_pos[j])) - r;
+                    min_image(P, dr);
+                    const float rr = dot3(dr, dr);
+                    if (rr > P.lj_rc2) continue;
+                    const float rr4 = rr * rr * rr * rr;
+                    const float rr7 = rr * rr * rr * rr * rr * rr * rr;
+                    const float fm = P.lj_amp * ((P.lj_two_s6 / rr7) - (1.0f / rr4));
+                    f.x -= fm * dr.x;
+                    f.y -= fm * dr.y;
+                    f.z -= fm * dr.z;
+                }
+            }
+    float4 F = S.force[me];
+    F.x += f.x;
+    F.y += f.y;
+    F.z += f.z;
+    S.force[me] = F;
+    if (!finite3(f3(F))) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
+}
+
+__global__ void __launch_bounds__(256) srd_hash_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
+                                                       int shift_from_step, float3 shift)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.ntotal) return;
+    if (shift_from_step) shift = srd_shift_of(P, *S.step_base + step_off);
+    const uint32_t h = srd_hash(P, f3(S.pos[i]), shift);
+    S.srd_hash[i] = h;
+    S.srd_slot[i] = count_into_cell(S.srd_count, S.srd_chunk, h);
+}
+
+__global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
+                                                          float dt_srd)
+{
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= P.srd_ncells) return;
+    const unsigned long long step = *S.step_base + step_off;
+    const uint32_t lo = S.srd_offset[c], hi = S.srd_offset[c + 1];
+    const uint32_t n = hi - lo;
+    float3 u = zero3();
+    if (n > 0) {
+        // stable member order
+        uint32_t ids[kSrdLocal];
+        const bool local = n <= kSrdLocal;
+        const bool exact = n <= kStableCap;
+        if (!exact) atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
+        if (local) {
+            for (uint32_t k = 0; k < n; ++k) {
+                const uint32_t x = S.srd_tmp[lo + k];
+                uint32_t m = k;
+                while (m > 0 && ids[m - 1] > x) {
+                    ids[m] = ids[m - 1];
+                    --m;
+                }
+                ids[m] = x;
+            }
+            for (uint32_t k = 0; k < n; ++k) S.srd_sorted_index[lo + k] = ids[k];
+        } else {
+            for (uint32_t q = lo; q < hi; ++q) {
+                const uint32_t x = S.srd_tmp[q];
+                const uint32_t rnk = exact ? bucket_rank(S.srd_tmp, lo, hi, x, q, S.err) : q - lo;
+                S.srd_sorted_index[lo + rnk] = x;
+            }
+        }
+        // after this point members are read back in stable order
+        auto member = [&](uint32_t k) -> uint32_t { return local ? ids[k] : S.srd_sorted_index[lo + k]; };
+        if (P.srd_thermo == NW_SRD_THERMO_REF_LAB) {
+            float E = 0.f;
+            for (uint32_t k = 0; k < n; ++k) {
+                const float4 V = S.vel[member(k)];
+                const float3 v = f3(V);
+                E += (0.5f * V.w) * dot3(v, v);
+            }
+            const float lam = sqrtf(P.srd_kT / E);
+            for (uint32_t k = 0; k < n; ++k) {
+                const uint32_t id = member(k);
+                const float4 V = S.vel[id];
+                S.vel[id] = make_float4(lam * V.x, lam * V.y, lam * V.z, V.w);
+            }
+        }
+        float M = 0.f;
+        for (uint32_t k = 0; k < n; ++k) {
+            const float4 V = S.vel[member(k)];
+            u += V.w * f3(V);
+            M += V.w;
+        }
+        if (M > 0.f) {
+            const float inv = 1.0f / M;
+            u = u * inv;
+        }
+        const int sign = 2 * (int)(u01(rng_draw(P, c, step, kRngSrdRot).x) > 0.5f) - 1;
+        const float ang = (float)sign * P.srd_alpha;
+        const float sa = sinf(ang), ca = cosf(ang);
+        uint32_t nrot = 0;
+        float ke = 0.f;
+        for (uint32_t k = 0; k < n; ++k) {
+            const uint32_t id = member(k);
+            if (id < P.nb && !P.srd_rotate_beads) continue;
+            const float4 V = S.vel[id];
+            const float3 d = f3(V) - u;
+            const float rx = d.x * ca - d.y * sa;
+            const float ry = d.x * sa + d.y * ca;
+            S.vel[id] = make_float4(u.x + rx, u.y + ry, u.z + d.z, V.w);
+            ke += (0.5f * V.w) * (rx * rx + ry * ry);
+            ++nrot;
+        }
+        if (P.srd_thermo == NW_SRD_THERMO_CELL_REL && nrot >= 2u && ke > 0.f) {
+            const float lam = sqrtf(((float)(nrot - 1u) * P.srd_kT) / ke);
+            for (uint32_t k = 0; k < n; ++k) {
+                const uint32_t id = member(k);
+                if (id < P.nb && !P.srd_rotate_beads) continue;
+                const float4 V = S.vel[id];
+                S.vel[id] = make_float4(u.x + lam * (V.x - u.x), u.y + lam * (V.y - u.y), V.z, V.w);
+            }
+        }
+        for (uint32_t k = 0; k < n; ++k) {
+            const uint32_t id = member(k);
+            if (id < P.nb) continue;
+            const float4 P4 = S.pos[id];
+            const float4 V4 = S.vel[id];
+            float3 p = f3(P4), v = f3(V4);
+            const float3 dr = dt_srd * v;
+            p += dr;
+            apply_boundaries(P, p, v, dr, 0.0f);
+            S.pos[id] = make_float4(p.x, p.y, p.z, P4.w);
+            S.vel[id] = make_float4(v.x, v.y, v.z, V4.w);
+        }
+    }
+    S.srd_mean[c] = make_float4(u.x, u.y, u.z, 0.f);
+}
+
+__global__ void advance_step_kernel(unsigned long long* step_base, unsigned long long k) { *step_base += k; }
+
+}  // namespace nw

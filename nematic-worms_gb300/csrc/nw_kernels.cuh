@@ -1,0 +1,376 @@
+// nw_kernels.cuh — the step kernels of the GB300 worm engine.
+//
+// One step is five launches (plus four every srd_gap steps):
+//   filament_pass   integrate + [reverse] + Langevin + bending/tangents
+//                   [+ bonds + drive] + cell hash + counting-sort slot
+//   scan_cells      cell offsets / starts / ends from the cell counts
+//   scatter         bucket the bead indices by cell
+//   stable_gather   order every bucket by index (the stable sort) and
+//                   gather positions (+ velocities and tangents) in cell order
+//   pair_*          pair forces over the 3x3(x3) neighbour cells
+//   [srd_hash, scan_cells, scatter, srd_collide]
+//
+// No float atomics are used anywhere: every output element has exactly one
+// writer, so repeated runs are bit-identical.
+#pragma once
+
+#include "nw_device.cuh"
+
+namespace nw {
+
+// Beyond these occupancies a cell is reported (NW_EFLAG_CELL_OVERFLOW) and
+// processed with bounded work; physical states never get close.
+constexpr uint32_t kStableCap = 128;  // members ordered exactly up to this count
+constexpr uint32_t kPairCap = 1024;   // members scanned per neighbour cell
+constexpr uint32_t kSrdLocal = 32;    // SRD members kept in registers
+
+struct StepBuffers {
+    float4 *pos, *vel, *force, *force_old, *tangent;
+    uint32_t *hash, *slot, *tmp_index, *sorted_index, *sorted_hash;
+    uint32_t *cell_count, *cell_offset, *cell_start, *cell_end, *chunk_count;
+    float4 *sorted_pos, *sorted_vel, *sorted_tan;
+    uint32_t *srd_hash, *srd_slot, *srd_tmp, *srd_sorted_index;
+    uint32_t *srd_count, *srd_offset, *srd_start, *srd_end, *srd_chunk;
+    float4* srd_mean;
+    uint32_t* err;
+    unsigned long long* step_base;
+};
+
+__device__ __forceinline__ uint32_t warp_sum(uint32_t x)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    return x;
+}
+
+// Count one element into its cell and, warp-aggregated, into its chunk.
+__device__ __forceinline__ uint32_t count_into_cell(uint32_t* cell_count, uint32_t* chunk_count, uint32_t h)
+{
+    const uint32_t slot = atomicAdd(&cell_count[h], 1u);
+    const uint32_t ck = h >> kChunkLog2;
+    const uint32_t am = __activemask();
+    const uint32_t peers = __match_any_sync(am, ck);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&chunk_count[ck], (uint32_t)__popc(peers));
+    return slot;
+}
+
+// ---- bonded helpers ----------------------------------------------------------
+
+// One bending triple (filamentKernel, particles_kernel_impl.cuh:777-800).
+struct Triple {
+    float3 fi, fj, fk;
+};
+__device__ __forceinline__ Triple bend_triple(const DevParams& P, float3 ri, float3 rj, float3 rk)
+{
+    float3 rij = rj - ri, rjk = rk - rj;
+    const float dij = min_image_len(P, rij);
+    const float djk = min_image_len(P, rjk);
+    const float dd = dot3(rij, rjk);
+    const float A = P.bend_k / (dij * djk);
+    const float3 B = (rij * dd) / dot3(rij, rij);
+    const float3 C = (rjk * dd) / dot3(rjk, rjk);
+    Triple t;
+    t.fi = (-A) * (rjk - B);
+    t.fk = (-A) * (C - rij);
+    t.fj = (-t.fi) - t.fk;
+    return t;
+}
+
+// getTangent (particles_kernel_impl.cuh:303-309).
+__device__ __forceinline__ float3 tangent_of(const DevParams& P, float3 a, float3 b)
+{
+    float3 rel = b - a;
+    const float d = min_image_len(P, rel);
+    return rel / d;
+}
+
+// Archived harmonic bond (NWWormsKernel_InternalForce.h:37-59).
+__device__ __forceinline__ void wca_bond(const DevParams& P, float3 ri, float3 rj, float3& f)
+{
+    float3 dr = rj - ri;
+    min_image(P, dr);
+    const float r = sqrtf(dot3(dr, dr));
+    const float fm = -(P.bond_k * (r - P.bond_r0)) / r;
+    f.x -= fm * dr.x;
+    f.y -= fm * dr.y;
+    f.z -= fm * dr.z;
+}
+
+// Archived tangent drive (NWWormsKernel_DriveForce.h:21-34).
+__device__ __forceinline__ void wca_drive(const DevParams& P, float3 ri, float3 rn, float3& f)
+{
+    float3 dr = rn - ri;
+    min_image(P, dr);
+    const float m = sqrtf(dot3(dr, dr));
+    f.x += P.activity * (dr.x / m);
+    f.y += P.activity * (dr.y / m);
+    f.z += P.activity * (dr.z / m);
+}
+
+// ---- K1: filament pass ---------------------------------------------------------
+// A block owns `fpb` whole filaments (beads [w0*L, (w0+fpb)*L) in storage
+// order), so reversal and every bonded term stay inside the block's shared
+// memory.  Follows ParticleSystem::update steps integrate -> reverse ->
+// Langevin -> filamentForces -> calcHash (simulation/particleSystem.cpp:257-299).
+__global__ void __launch_bounds__(1024) filament_pass_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
+                                                             float dt, uint32_t fpb);
+
+// ---- K2: cell scan ---------------------------------------------------------------
+// Block b scans cells [b*4096, (b+1)*4096); the counts of all earlier chunks
+// were accumulated by the producer, so no block waits on another.
+// offset[c] = exclusive prefix, offset[ncells] = total; start/end in the
+// reference's format (0xffffffff for empty cells); counts are reset to zero.
+template <bool kBounds>
+__global__ void __launch_bounds__(512) scan_cells_kernel(uint32_t* __restrict__ count,
+                                                         const uint32_t* __restrict__ chunk_count, uint32_t ncells,
+                                                         uint32_t* __restrict__ offset, uint32_t* __restrict__ start,
+                                                         uint32_t* __restrict__ end)
+{
+    __shared__ uint32_t s_w[16];
+    __shared__ uint32_t s_base;
+    const uint32_t b = blockIdx.x, tid = threadIdx.x, lane = tid & 31u, wid = tid >> 5;
+    uint32_t part = 0;
+    for (uint32_t k = tid; k < b; k += 512u) part += chunk_count[k];
+    part = warp_sum(part);
+    if (lane == 0) s_w[wid] = part;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t x = lane < 16u ? s_w[lane] : 0u;
+        x = warp_sum(x);
+        if (lane == 0) s_base = x;
+    }
+    __syncthreads();
+    const uint32_t base = s_base;
+    __syncthreads();
+
+    const uint32_t c0 = b * kChunk + tid * 8u;
+    uint32_t cnt[8];
+    uint32_t tot = 0;
+    if (c0 + 8u <= ncells) {
+        const uint4 a = *reinterpret_cast<const uint4*>(count + c0);
+        const uint4 d = *reinterpret_cast<const uint4*>(count + c0 + 4);
+        cnt[0] = a.x; cnt[1] = a.y; cnt[2] = a.z; cnt[3] = a.w;
+        cnt[4] = d.x; cnt[5] = d.y; cnt[6] = d.z; cnt[7] = d.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) cnt[k] = (c0 + k < ncells) ? count[c0 + k] : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) tot += cnt[k];
+    const uint32_t incl = warp_incl_scan(tot);
+    if (lane == 31u) s_w[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        const uint32_t x = lane < 16u ? s_w[lane] : 0u;
+        const uint32_t xi = warp_incl_scan(x);
+        if (lane < 16u) s_w[lane] = xi - x;
+    }
+    __syncthreads();
+    uint32_t run = base + s_w[wid] + incl - tot;
+    if (c0 + 8u <= ncells) {
+        uint32_t o[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            o[k] = run;
+            run += cnt[k];
+        }
+        *reinterpret_cast<uint4*>(offset + c0) = make_uint4(o[0], o[1], o[2], o[3]);
+        *reinterpret_cast<uint4*>(offset + c0 + 4) = make_uint4(o[4], o[5], o[6], o[7]);
+        if (kBounds) {
+            uint32_t s[8], e[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                s[k] = cnt[k] ? o[k] : kEmpty;
+                e[k] = cnt[k] ? o[k] + cnt[k] : kEmpty;
+            }
+            *reinterpret_cast<uint4*>(start + c0) = make_uint4(s[0], s[1], s[2], s[3]);
+            *reinterpret_cast<uint4*>(start + c0 + 4) = make_uint4(s[4], s[5], s[6], s[7]);
+            *reinterpret_cast<uint4*>(end + c0) = make_uint4(e[0], e[1], e[2], e[3]);
+            *reinterpret_cast<uint4*>(end + c0 + 4) = make_uint4(e[4], e[5], e[6], e[7]);
+        }
+        *reinterpret_cast<uint4*>(count + c0) = make_uint4(0u, 0u, 0u, 0u);
+        *reinterpret_cast<uint4*>(count + c0 + 4) = make_uint4(0u, 0u, 0u, 0u);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t c = c0 + k;
+            if (c < ncells) {
+                offset[c] = run;
+                if (kBounds) {
+                    start[c] = cnt[k] ? run : kEmpty;
+                    end[c] = cnt[k] ? run + cnt[k] : kEmpty;
+                }
+                count[c] = 0u;
+            }
+            run += cnt[k];
+        }
+    }
+    if (c0 < ncells && c0 + 8u >= ncells) offset[ncells] = run;
+}
+
+// ---- K3: scatter into cell buckets (arbitrary order inside a bucket) -------------
+__global__ void __launch_bounds__(256) scatter_kernel(const uint32_t* __restrict__ hash,
+                                                      const uint32_t* __restrict__ slot,
+                                                      const uint32_t* __restrict__ offset, uint32_t* __restrict__ tmp,
+                                                      uint32_t n, uint32_t* __restrict__ chunk_count, uint32_t nchunks);
+
+// Rank of element `i` among the members of its bucket (= stable position).
+__device__ __forceinline__ uint32_t bucket_rank(const uint32_t* __restrict__ tmp, uint32_t lo, uint32_t hi, uint32_t i,
+                                                uint32_t q, uint32_t* err)
+{
+    if (hi - lo > kStableCap) {
+        if (q == lo) atomicOr(err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
+        return q - lo;
+    }
+    uint32_t r = 0;
+    for (uint32_t k = lo; k < hi; ++k) r += tmp[k] < i;
+    return r;
+}
+
+// ---- K4: stable order + gather ---------------------------------------------------
+// Completes the stable sort (thrust::sort_by_key order: by hash, ties by
+// index) and performs reorderDataAndFindCellStartD's gather
+// (particles_kernel_impl.cuh:406-420).
+template <bool kRef>
+__global__ void __launch_bounds__(256) stable_gather_kernel(const DevParams P, const StepBuffers S)
+{
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= P.nb) return;
+    const uint32_t i = S.tmp_index[q];
+    const uint32_t h = S.hash[i];
+    const uint32_t lo = S.cell_offset[h], hi = S.cell_offset[h + 1];
+    const uint32_t d = lo + bucket_rank(S.tmp_index, lo, hi, i, q, S.err);
+    S.sorted_index[d] = i;
+    S.sorted_hash[d] = h;
+    S.sorted_pos[d] = S.pos[i];
+    if (kRef) {
+        S.sorted_vel[d] = S.vel[i];
+        S.sorted_tan[d] = S.tangent[i];
+    }
+}
+
+// ---- K5: pair forces ---------------------------------------------------------------
+
+// collideCell for one neighbour cell (particles_kernel_impl.cuh:492-556).
+__device__ __forceinline__ float3 ref_cell_sum(const DevParams& P, const StepBuffers& S, uint32_t h, uint32_t p,
+                                               float3 r, float3 v, float3 t, uint32_t fI, uint32_t cI)
+{
+    float3 sum = zero3();
+    const uint32_t s0 = __ldg(&S.cell_start[h]);
+    if (s0 == kEmpty) return sum;
+    uint32_t s1 = __ldg(&S.cell_end[h]);
+    if (s1 - s0 > kPairCap) {
+        atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
+        s1 = s0 + kPairCap;
+    }
+    const float cd = P.radius + P.radius;
+    for (uint32_t j = s0; j < s1; ++j) {
+        if (j == p) continue;
+        const float3 r2 = f3(__ldg(&S.sorted_pos[j]));
+        const float3 v2 = f3(__ldg(&S.sorted_vel[j]));
+        const float3 t2 = f3(__ldg(&S.sorted_tan[j]));
+        const uint32_t o = __ldg(&S.sorted_index[j]);
+        const uint32_t fJ = o / P.L, cJ = o - fJ * P.L;
+        const bool same = fI == fJ;
+        if (same && ((cI + 1u == cJ) || (cI - 1u == cJ))) {
+            // bondHookean (:466-473)
+            float3 rel = r2 - r;
+            const float d = min_image_len(P, rel);
+            const float3 n = rel / d;
+            sum += (-P.bond_k * (P.bond_r0 - d)) * n;
+        } else {
+            // collideParticles (:427-462)
+            float3 rel = r2 - r;
+            const float d = min_image_len(P, rel);
+            if (d < cd) {
+                const float3 n = rel / d;
+                const float3 rv = v2 - v;
+                const float3 tv = rv - dot3(rv, n) * n;
+                float3 F = (-P.spring * (cd - d)) * n;
+                F += P.damping * rv;
+                F += P.shear * tv;
+                sum += F;
+            }
+        }
+        if (!same) {
+            // extensileForce (:477-487)
+            float3 rel = r2 - r;
+            const float d = min_image_len(P, rel);
+            if (dot3(t, t2) < -0.5f) sum += ((-P.activity) * (t - t2)) / (2.0f * d);
+        }
+    }
+    return sum;
+}
+
+// REF_DEM: collideFilamentsKernel (particles_kernel_impl.cuh:694-744).  With a
+// single z layer every (x, y) neighbour cell is reached by all three z
+// offsets; its sum is computed once and added three times in the reference's
+// z, y, x order, which reproduces the reference's accumulation exactly.
+__global__ void __launch_bounds__(256) pair_ref_kernel(const DevParams P, const StepBuffers S);
+
+// Distinct neighbour cells of one axis under modulo wrap (or clipping at walls),
+// in increasing offset order.
+__device__ __forceinline__ int axis_cells(const DevParams& P, int a, uint32_t c, uint32_t out[3])
+{
+    const int G = (int)P.grid[a];
+    int n = 0;
+#pragma unroll
+    for (int o = -1; o <= 1; ++o) {
+        int x = (int)c + o;
+        if (P.bnd[a] == NW_PERIODIC) {
+            if (x < 0) x += G;
+            else if (x >= G) x -= G;
+        } else if (x < 0 || x >= G) {
+            continue;
+        }
+        bool dup = false;
+        for (int k = 0; k < n; ++k) dup |= out[k] == (uint32_t)x;
+        if (!dup) out[n++] = (uint32_t)x;
+    }
+    return n;
+}
+
+// WCA_WORMS pair pass: repulsive LJ to every bead within lj_rcut in the
+// distinct neighbour cells, except same-filament pairs |i - j| <= lj_exclude
+// (NWWormsKernel_LennardJones.h:38-50, NWWormsKernel_InternalForce.h:196-208,
+// NWDeviceFunctions.h:73-76).
+__global__ void __launch_bounds__(256) pair_wca_kernel(const DevParams P, const StepBuffers S);
+
+// ---- SRD -------------------------------------------------------------------------
+
+// Random grid shift of the collision at `step`: (lo + U) * cell per axis,
+// no z shift in 2D (the reference draws frand() * cell for x and y,
+// simulation/particleSystem.cpp:345-346).
+__device__ __forceinline__ float3 srd_shift_of(const DevParams& P, unsigned long long step)
+{
+    const uint4 x = rng_draw(P, 0u, step, kRngSrdShift);
+    return make_float3((P.srd_shift_lo + u01(x.x)) * P.srd_cell[0], (P.srd_shift_lo + u01(x.y)) * P.srd_cell[1],
+                       P.dim >= 3 ? (P.srd_shift_lo + u01(x.z)) * P.srd_cell[2] : 0.0f);
+}
+
+// calcHashD(srd = true) over beads and solvent + counting-sort slot.
+__global__ void __launch_bounds__(256) srd_hash_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
+                                                       int shift_from_step, float3 shift);
+
+// One SRD cell per thread: members in stable (index) order, then the
+// reference's isokinetic thermostat (particles_kernel_impl.cuh:605-637) or
+// none, the mass-weighted cell mean (:560-594), the +/- alpha rotation of
+// (v - u) (:640-691), the relative-velocity thermostat when selected, and the
+// solvent's ballistic streaming by dt_srd (solvent_integrator, :145-205).
+__global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
+                                                          float dt_srd);
+
+__global__ void advance_step_kernel(unsigned long long* step_base, unsigned long long k);
+
+}  // namespace nw

@@ -1,0 +1,141 @@
+// nw_sort.cuh — general stable key/value sort (LSD radix, 8-bit digits) for
+// arbitrary 32-bit keys.  The step itself uses the cell counting sort of
+// nw_kernels.cuh; this sort backs the legacy sortParticles symbol
+// (simulation/particleSystem_cuda.cu:277-282, thrust::sort_by_key), whose
+// keys are not known to be cell indices.
+#pragma once
+
+#include "nw_kernels.cuh"
+
+namespace nw {
+
+constexpr uint32_t kRadixThreads = 256;
+constexpr uint32_t kRadixItems = 8;
+constexpr uint32_t kRadixTile = kRadixThreads * kRadixItems;  // 2048 keys per block
+
+// Digit histogram of one tile: ghist[d * nblocks + b].
+__global__ void __launch_bounds__(256) radix_hist_kernel(const uint32_t* __restrict__ keys, uint32_t n, int shift,
+                                                         uint32_t* __restrict__ ghist, uint32_t nblocks)
+{
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * kRadixTile;
+#pragma unroll
+    for (uint32_t r = 0; r < kRadixItems; ++r) {
+        const uint32_t e = base + r * kRadixThreads + threadIdx.x;
+        if (e < n) atomicAdd(&h[(keys[e] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    ghist[threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+// Sum of each 4096-entry chunk of an array (feeds scan_cells_kernel).
+__global__ void __launch_bounds__(512) chunk_sum_kernel(const uint32_t* __restrict__ a, uint32_t m,
+                                                        uint32_t* __restrict__ chunk)
+{
+    __shared__ uint32_t s_w[16];
+    const uint32_t c0 = blockIdx.x * kChunk;
+    uint32_t x = 0;
+    for (uint32_t k = threadIdx.x; k < kChunk; k += 512u)
+        if (c0 + k < m) x += a[c0 + k];
+    x = warp_sum(x);
+    if ((threadIdx.x & 31u) == 0) s_w[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint32_t y = threadIdx.x < 16 ? s_w[threadIdx.x] : 0u;
+        y = warp_sum(y);
+        if (threadIdx.x == 0) chunk[blockIdx.x] = y;
+    }
+}
+
+// Stable scatter of one tile: rounds of 256 consecutive keys; inside a round
+// the rank of a key among equal digits is (earlier warps' counts) + (earlier
+// lanes of its warp), so input order is kept.
+__global__ void __launch_bounds__(256) radix_scatter_kernel(const uint32_t* __restrict__ kin,
+                                                            const uint32_t* __restrict__ vin,
+                                                            uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                            uint32_t n, int shift,
+                                                            const uint32_t* __restrict__ goffset, uint32_t nblocks)
+{
+    __shared__ uint32_t s_base[256];
+    __shared__ uint32_t s_run[256];
+    __shared__ uint32_t s_cnt[8][257];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    s_base[tid] = goffset[tid * nblocks + blockIdx.x];
+    s_run[tid] = 0;
+    const uint32_t lt = (1u << lane) - 1u;
+    const uint32_t base = blockIdx.x * kRadixTile;
+    for (uint32_t r = 0; r < kRadixItems; ++r) {
+#pragma unroll
+        for (int w = 0; w < 8; ++w) s_cnt[w][tid] = 0;
+        if (tid == 0)
+            for (int w = 0; w < 8; ++w) s_cnt[w][256] = 0;
+        __syncthreads();
+        const uint32_t e = base + r * kRadixThreads + tid;
+        const bool valid = e < n;
+        const uint32_t key = valid ? kin[e] : 0u;
+        const uint32_t d = valid ? ((key >> shift) & 255u) : 256u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t rank = __popc(peers & lt);
+        if (rank == 0) s_cnt[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            uint32_t before = 0;
+            for (uint32_t w = 0; w < warp; ++w) before += s_cnt[w][d];
+            const uint32_t pos = s_base[d] + s_run[d] + before + rank;
+            kout[pos] = key;
+            vout[pos] = vin[e];
+        }
+        __syncthreads();
+        uint32_t add = 0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) add += s_cnt[w][tid];
+        s_run[tid] += add;
+        __syncthreads();
+    }
+}
+
+// Scratch of one radix sort of up to `capacity` keys.
+struct RadixScratch {
+    uint32_t* keys_alt = nullptr;
+    uint32_t* vals_alt = nullptr;
+    uint32_t* ghist = nullptr;
+    uint32_t* goffset = nullptr;
+    uint32_t* chunk = nullptr;
+    uint32_t capacity = 0;
+};
+
+// Bytes of scratch a sort of n keys needs, split as RadixScratch uses them.
+inline size_t radix_scratch_words(uint32_t n, size_t* hist_words, size_t* chunk_words)
+{
+    const size_t nblocks = (n + kRadixTile - 1) / kRadixTile;
+    const size_t m = 256 * (nblocks ? nblocks : 1);
+    *hist_words = m + 8;
+    *chunk_words = (m + kChunk - 1) / kChunk + 1;
+    return 2 * (size_t)n + 2 * (*hist_words) + (*chunk_words);
+}
+
+// Sort (keys, vals) in place, stable, 4 passes; scratch must hold n keys.
+inline void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, const RadixScratch& S, cudaStream_t s)
+{
+    if (n < 2) return;
+    const uint32_t nblocks = (n + kRadixTile - 1) / kRadixTile;
+    const uint32_t m = 256u * nblocks;
+    const uint32_t nchunks = (m + kChunk - 1) / kChunk;
+    uint32_t *ki = keys, *vi = vals, *ko = S.keys_alt, *vo = S.vals_alt;
+    for (int shift = 0; shift < 32; shift += 8) {
+        radix_hist_kernel<<<nblocks, 256, 0, s>>>(ki, n, shift, S.ghist, nblocks);
+        chunk_sum_kernel<<<nchunks, 512, 0, s>>>(S.ghist, m, S.chunk);
+        scan_cells_kernel<false><<<nchunks, 512, 0, s>>>(S.ghist, S.chunk, m, S.goffset, nullptr, nullptr);
+        radix_scatter_kernel<<<nblocks, 256, 0, s>>>(ki, vi, ko, vo, n, shift, S.goffset, nblocks);
+        uint32_t* t = ki;
+        ki = ko;
+        ko = t;
+        t = vi;
+        vi = vo;
+        vo = t;
+    }
+}
+
+}  // namespace nw

@@ -1,0 +1,248 @@
+"""Host-side mirror of the engine's C ABI.
+
+``System`` wraps the handle API of include/nwgb.h (one simulated system on
+one GPU).  ``ParticleSystem`` mirrors the reference's host class
+(simulation/particleSystem.h:24-211): same method names, argument meaning and
+defaults, so scripts written against the reference read the same here.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .abi import NwConfig, check
+
+_FLOAT4 = {abi.NW_POSITION, abi.NW_VELOCITY, abi.NW_TANGENT, abi.NW_FORCE, abi.NW_FORCE_OLD, abi.NW_SRD_CELL_MEAN}
+
+
+class System:
+    """One system on the current CUDA device (nw_create / nw_destroy)."""
+
+    def __init__(self, cfg: NwConfig, lib: C.CDLL | None = None):
+        self.lib = lib or abi.load_library()
+        self._h = C.c_void_p()
+        check(self.lib.nw_create(C.byref(cfg), C.byref(self._h)), "nw_create")
+        nb, ns, nc, nsc = C.c_uint32(), C.c_uint32(), C.c_uint32(), C.c_uint32()
+        check(self.lib.nw_get_counts(self._h, C.byref(nb), C.byref(ns), C.byref(nc), C.byref(nsc)))
+        self.n_beads, self.n_solvent, self.n_cells, self.n_srd_cells = nb.value, ns.value, nc.value, nsc.value
+
+    # -- lifetime -----------------------------------------------------------------
+    def close(self) -> None:
+        if self._h:
+            check(self.lib.nw_destroy(self._h), "nw_destroy")
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- configuration ----------------------------------------------------------------
+    @property
+    def config(self) -> NwConfig:
+        c = NwConfig()
+        check(self.lib.nw_get_config(self._h, C.byref(c)))
+        return c
+
+    def set_config(self, cfg: NwConfig) -> None:
+        check(self.lib.nw_set_config(self._h, C.byref(cfg)), "nw_set_config")
+
+    # -- arrays ---------------------------------------------------------------------------
+    def _size(self, which: int) -> int:
+        if which in (abi.NW_POSITION, abi.NW_VELOCITY):
+            return self.n_beads + self.n_solvent
+        if which in (abi.NW_TANGENT, abi.NW_FORCE, abi.NW_FORCE_OLD, abi.NW_HASH, abi.NW_SORTED_INDEX):
+            return self.n_beads
+        if which in (abi.NW_CELL_START, abi.NW_CELL_END):
+            return self.n_cells
+        if which == abi.NW_SRD_SORTED_INDEX:
+            return self.n_beads + self.n_solvent
+        return self.n_srd_cells
+
+    def set_array(self, which: int, data, start: int = 0) -> None:
+        if which in _FLOAT4:
+            a = np.ascontiguousarray(np.asarray(data, dtype=np.float32).reshape(-1, 4))
+        else:
+            a = np.ascontiguousarray(np.asarray(data, dtype=np.uint32).reshape(-1))
+        check(self.lib.nw_set_array(self._h, which, a.ctypes.data, start, a.shape[0]), "nw_set_array")
+
+    def get_array(self, which: int, start: int = 0, count: int | None = None) -> np.ndarray:
+        if count is None:
+            count = self._size(which) - start
+        if which in _FLOAT4:
+            out = np.empty((count, 4), dtype=np.float32)
+        else:
+            out = np.empty(count, dtype=np.uint32)
+        check(self.lib.nw_get_array(self._h, which, out.ctypes.data, start, count), "nw_get_array")
+        return out
+
+    def device_ptr(self, which: int) -> int:
+        p = C.c_void_p()
+        check(self.lib.nw_device_array(self._h, which, C.byref(p)), "nw_device_array")
+        return p.value or 0
+
+    def zero_forces(self) -> None:
+        check(self.lib.nw_zero_forces(self._h), "nw_zero_forces")
+
+    # -- stepping ---------------------------------------------------------------------------
+    def step(self, n: int = 1, dt: float = 0.0) -> None:
+        check(self.lib.nw_step(self._h, int(n), float(dt)), "nw_step")
+
+    def sync(self) -> None:
+        check(self.lib.nw_sync(self._h), "nw_sync")
+
+    def error_word(self) -> int:
+        f = C.c_uint32()
+        check(self.lib.nw_error_word(self._h, C.byref(f)))
+        return f.value
+
+    @property
+    def step_index(self) -> int:
+        s = C.c_uint64()
+        check(self.lib.nw_get_step(self._h, C.byref(s)))
+        return s.value
+
+    def set_step(self, step: int) -> None:
+        check(self.lib.nw_set_step(self._h, int(step)))
+
+    def set_graphs(self, enabled: bool) -> None:
+        check(self.lib.nw_set_graphs(self._h, 1 if enabled else 0))
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        check(self.lib.nw_set_stream(self._h, C.c_void_p(stream_handle or 0)))
+
+    def srd_collide(self, dt_srd: float, shift) -> None:
+        s = (C.c_float * 3)(*[float(x) for x in shift])
+        check(self.lib.nw_srd_collide(self._h, float(dt_srd), s), "nw_srd_collide")
+
+    @property
+    def last_launch_count(self) -> int:
+        n = C.c_uint64()
+        check(self.lib.nw_last_launch_count(self._h, C.byref(n)))
+        return n.value
+
+    # -- checkpoints ------------------------------------------------------------------------
+    def checkpoint(self) -> bytes:
+        n = C.c_size_t()
+        check(self.lib.nw_checkpoint_size(self._h, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        check(self.lib.nw_checkpoint_save(self._h, buf, n.value), "nw_checkpoint_save")
+        return buf.raw
+
+    def restore(self, blob: bytes) -> None:
+        buf = C.create_string_buffer(blob, len(blob))
+        check(self.lib.nw_checkpoint_load(self._h, buf, len(blob)), "nw_checkpoint_load")
+
+
+class ParticleSystem:
+    """Mirror of the reference's ParticleSystem (simulation/particleSystem.h:24-211).
+
+    ``ParticleSystem(numFilaments, filamentSize, gridSize, srdSolvent)`` builds
+    the REF_DEM configuration with the reference constructor's defaults;
+    setters change the host-side parameters, which are uploaded on the next
+    ``update`` (simulation/particleSystem.cpp:255).
+    """
+
+    POSITION, VELOCITY, TANGENT = 0, 1, 2
+
+    def __init__(self, numFilaments: int, filamentSize: int, gridSize=(1024, 128, 1), srdSolvent: bool = False,
+                 cfg: NwConfig | None = None):
+        self._cfg = cfg.copy() if cfg is not None else abi.default_config(
+            abi.NW_MODEL_REF_DEM, numFilaments, filamentSize, tuple(gridSize), srdSolvent)
+        self._sys = System(self._cfg)
+        self._dirty = False
+        self._sys.zero_forces()
+
+    # ParticleArray selectors map onto the engine's arrays
+    _ARR = {0: abi.NW_POSITION, 1: abi.NW_VELOCITY, 2: abi.NW_TANGENT}
+
+    @property
+    def system(self) -> System:
+        return self._sys
+
+    def getNumParticles(self) -> int:
+        return self._sys.n_beads
+
+    def update(self, deltaTime: float) -> None:
+        if self._dirty:
+            self._sys.set_config(self._cfg)
+            self._dirty = False
+        self._sys.step(1, deltaTime)
+
+    def getArray(self, array: int) -> np.ndarray:
+        """Bead data (n_beads x 4 floats), like the reference's getArray."""
+        return self._sys.get_array(self._ARR[array], 0, self._sys.n_beads)
+
+    def setArray(self, array: int, data, start: int, count: int) -> None:
+        a = np.asarray(data, dtype=np.float32).reshape(-1, 4)[:count]
+        self._sys.set_array(self._ARR[array], a, start)
+
+    def _set(self, **kw):
+        for k, v in kw.items():
+            setattr(self._cfg, k, v)
+        self._dirty = True
+
+    def setDamping(self, x):
+        self._set(gamma=x)
+
+    def setTemperature(self, x):
+        self._set(kT=x, srd_kT=x)
+
+    def setGravity(self, x):
+        self._cfg.gravity[1] = x
+        self._dirty = True
+
+    def setActivity(self, x):
+        self._set(activity=x)
+
+    def setReverseProbability(self, x):
+        self._set(reverse_probability=x)
+
+    def setCollideSpring(self, x):
+        self._set(spring=x)
+
+    def setCollideDamping(self, x):
+        self._set(damping=x)
+
+    def setCollideShear(self, x):
+        self._set(shear=x)
+
+    def setCollideAttraction(self, x):
+        self._set(attraction=x)
+
+    def setBondSpringConstant(self, x):
+        self._set(bond_k=x)
+
+    def setBondSpringLength(self, x):
+        self._set(bond_r0=x)
+
+    def setBondBendingConstant(self, x):
+        self._set(bend_k=x)
+
+    def setBoundaries(self, x, y, z):
+        self._cfg.boundary[0], self._cfg.boundary[1], self._cfg.boundary[2] = int(x), int(y), int(z)
+        self._dirty = True
+
+    def getParticleRadius(self) -> float:
+        return float(self._cfg.radius)
+
+    def getGridSize(self):
+        return tuple(int(g) for g in self._cfg.grid)
+
+    def getOrigin(self):
+        return tuple(float(o) for o in self._cfg.origin)
+
+    def getCellSize(self):
+        return tuple(float(c) for c in self._cfg.cell_size)
+
+    def close(self):
+        self._sys.close()

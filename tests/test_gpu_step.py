@@ -1,0 +1,186 @@
+"""Parity of the CUDA step (through the C ABI) with the CPU oracle.
+
+Tolerances: cell hashes, sort order and cell bounds bit-exact; positions,
+velocities and forces within 1e-5 of the FP32 oracle, measured as
+max |gpu - oracle| / max |oracle| per array; the FP64 oracle's error is
+reported alongside and bounded at 1e-4 (FP32 rounding of r^-14 terms).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from nwgb import abi
+from nwgb.init import initial_state, reference_reset, wca_config
+
+pytestmark = pytest.mark.gpu
+
+TOL32 = 1e-5
+TOL64 = 1e-4
+
+
+def make_case(kind: str, lib):
+    if kind == "wca":
+        cfg = wca_config(120, 10, (50.0, 50.0), seed=1, lib=lib)
+        pos, vel = initial_state(cfg, seed=1)
+        tan = np.zeros((cfg.n_beads, 4), np.float32)
+    elif kind == "wca_srd":
+        cfg = wca_config(80, 10, (40.0, 40.0), srd=True, seed=2, lib=lib)
+        pos, vel = initial_state(cfg, seed=2)
+        tan = np.zeros((cfg.n_beads, 4), np.float32)
+    elif kind == "wca_reverse":
+        cfg = wca_config(60, 12, (40.0, 40.0), seed=3, lib=lib)
+        cfg.reverse_probability = 0.4
+        pos, vel = initial_state(cfg, seed=3)
+        tan = np.zeros((cfg.n_beads, 4), np.float32)
+    elif kind in ("ref", "ref_srd", "ref_walls"):
+        srd = kind == "ref_srd"
+        cfg = abi.default_config(abi.NW_MODEL_REF_DEM, 150, 10, (64, 64, 1), srd, lib)
+        cfg.bond_r0 = 0.8
+        cfg.bend_k = 10.0
+        cfg.activity = 0.5
+        cfg.spring = 57.0
+        cfg.kT = 0.1
+        cfg.gamma = 2.0
+        cfg.srd_kT = 0.1
+        cfg.seed = 9
+        if kind == "ref_walls":
+            cfg.boundary[1] = abi.NW_WALL_NO_SLIP
+            cfg.boundary[2] = abi.NW_WALL
+        pos, vel, tan = reference_reset(cfg)
+        rng = np.random.default_rng(4)
+        pos[:cfg.n_beads, :2] += rng.normal(0, 0.05, (cfg.n_beads, 2)).astype(np.float32)
+    else:
+        raise ValueError(kind)
+    return cfg, pos, vel, tan
+
+
+def run_gpu(cfg, pos, vel, tan, nsteps=1, graphs=True):
+    import nwgb
+
+    s = nwgb.System(cfg)
+    s.set_graphs(graphs)
+    s.set_array(abi.NW_POSITION, pos)
+    s.set_array(abi.NW_VELOCITY, vel)
+    s.set_array(abi.NW_TANGENT, tan)
+    s.step(nsteps, cfg.dt)
+    s.sync()
+    out = {k: s.get_array(a) for k, a in (("pos", abi.NW_POSITION), ("vel", abi.NW_VELOCITY),
+                                           ("force", abi.NW_FORCE), ("force_old", abi.NW_FORCE_OLD),
+                                           ("tangent", abi.NW_TANGENT), ("hash", abi.NW_HASH),
+                                           ("sorted_index", abi.NW_SORTED_INDEX),
+                                           ("cell_start", abi.NW_CELL_START), ("cell_end", abi.NW_CELL_END))}
+    out["launches"] = s.last_launch_count
+    s.close()
+    return out
+
+
+def run_oracle(orc, cfg, pos, vel, tan, nsteps=1, prec=32):
+    z = np.zeros((cfg.n_beads, 4), np.float32)
+    st = dict(pos=pos, vel=vel, force=z, force_old=z, tangent=tan)
+    for k in range(nsteps):
+        st = orc.step(cfg, st, k, cfg.dt, prec)
+    return st
+
+
+CASES = ["wca", "wca_srd", "wca_reverse", "ref", "ref_srd", "ref_walls"]
+
+
+@pytest.mark.parametrize("kind", CASES)
+def test_one_step_matches_oracle(lib, orc, kind):
+    cfg, pos, vel, tan = make_case(kind, lib)
+    g = run_gpu(cfg, pos, vel, tan)
+    o = run_oracle(orc, cfg, pos, vel, tan, 1, 32)
+    o64 = run_oracle(orc, cfg, pos, vel, tan, 1, 64)
+    nb = cfg.n_beads
+    assert np.array_equal(g["hash"], o["hash"])
+    assert np.array_equal(g["sorted_index"], o["sorted_index"])
+    assert np.array_equal(g["cell_start"], o["cell_start"])
+    ne = o["cell_start"] != abi.EMPTY
+    assert np.array_equal(g["cell_end"][ne], o["cell_end"][ne])
+    for k in ("pos", "vel", "force", "force_old", "tangent"):
+        a = g[k][:nb] if k in ("pos", "vel") else g[k]
+        b = o[k][:nb] if k in ("pos", "vel") else o[k]
+        assert rel_err(a, b) < TOL32, (k, rel_err(a, b))
+        b64 = o64[k][:nb] if k in ("pos", "vel") else o64[k]
+        assert rel_err(a, b64) < TOL64, (k, "fp64", rel_err(a, b64))
+    if cfg.srd_enabled:  # solvent after the collision of step 0
+        assert rel_err(g["pos"][nb:], o["pos"][nb:]) < TOL32
+        assert rel_err(g["vel"][nb:], o["vel"][nb:]) < TOL32
+        assert g["launches"] == 5 + 4 + 1
+    else:
+        assert g["launches"] == 5 + 1
+
+
+@pytest.mark.parametrize("kind", ["wca", "ref_srd"])
+def test_graph_replay_is_bit_identical_to_direct_launches(lib, kind):
+    cfg, pos, vel, tan = make_case(kind, lib)
+    a = run_gpu(cfg, pos, vel, tan, nsteps=12, graphs=True)
+    b = run_gpu(cfg, pos, vel, tan, nsteps=12, graphs=False)
+    c = run_gpu(cfg, pos, vel, tan, nsteps=12, graphs=True)
+    for k in ("pos", "vel", "force", "tangent", "sorted_index"):
+        assert np.array_equal(a[k], b[k]), k
+        assert np.array_equal(a[k], c[k]), k  # run twice: no races
+
+
+@pytest.mark.parametrize("kind", ["wca", "wca_srd", "ref"])
+def test_short_trajectory_tracks_oracle(lib, orc, kind):
+    cfg, pos, vel, tan = make_case(kind, lib)
+    n = 12
+    g = run_gpu(cfg, pos, vel, tan, nsteps=n)
+    o = run_oracle(orc, cfg, pos, vel, tan, n, 32)
+    nb = cfg.n_beads
+    # trajectories separate only by accumulated FP32 rounding over 12 steps
+    assert rel_err(g["pos"][:nb], o["pos"][:nb]) < 1e-5
+    assert rel_err(g["force"], o["force"]) < 1e-3
+    assert np.mean(g["sorted_index"] == o["sorted_index"]) > 0.999
+
+
+def test_checkpoint_resume_is_bit_exact(lib):
+    import nwgb
+
+    cfg, pos, vel, tan = make_case("wca_srd", lib)
+    with nwgb.System(cfg) as s:
+        s.set_array(abi.NW_POSITION, pos)
+        s.set_array(abi.NW_VELOCITY, vel)
+        s.step(7, cfg.dt)
+        blob = s.checkpoint()
+        s.step(9, cfg.dt)
+        ref = s.get_array(abi.NW_POSITION)
+    with nwgb.System(cfg) as s2:
+        s2.restore(blob)
+        assert s2.step_index == 7
+        s2.step(9, cfg.dt)
+        assert np.array_equal(s2.get_array(abi.NW_POSITION), ref)
+
+
+def test_nonfinite_state_is_reported(lib):
+    import nwgb
+
+    cfg, pos, vel, tan = make_case("wca", lib)
+    pos = pos.copy()
+    pos[17, 0] = np.nan
+    with nwgb.System(cfg) as s:
+        s.set_array(abi.NW_POSITION, pos)
+        s.set_array(abi.NW_VELOCITY, vel)
+        s.step(1, cfg.dt)
+        with pytest.raises(nwgb.NwError) as e:
+            s.sync()
+        assert e.value.status == abi.NW_ERR_NONFINITE
+        # the context stays usable: a clean state steps without error
+        p2, _ = initial_state(cfg, seed=1)
+        s.set_array(abi.NW_POSITION, p2)
+        s.zero_forces()
+        s.step(2, cfg.dt)
+        s.sync()
+
+
+def test_empty_system_steps(lib):
+    import nwgb
+
+    cfg = wca_config(0, 10, (20.0, 20.0), lib=lib)
+    with nwgb.System(cfg) as s:
+        s.step(3, cfg.dt)
+        s.sync()
+        assert s.step_index == 3
