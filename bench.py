@@ -1,0 +1,382 @@
+#!/usr/bin/env python
+"""bench.py — bead-steps/s of the nematic-worm step on GB300.
+
+Workload (default): 2D WCA worms with SRD solvent, 20,000 worms x 20 beads =
+400,000 beads in a periodic 1000 x 1000 box, 4,000,000 SRD particles (density
+4 per unit cell), SRD collision every 10 steps, FP32, dt = 0.005.  A step is
+one ParticleSystem::update equivalent (the SRD sub-step every 10th step).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Our arm: K steps replayed from CUDA graphs of 10 steps (one SRD period), timed
+with CUDA events on the engine's stream between a barrier + synchronize on
+both sides; the state (~190 MB) is larger than L2.  Under torchrun every rank
+runs an independent replica ("replicas only": a single system is not sharded)
+and `value` is the sum over ranks.  Reference arm: the CPU port of the
+reference's step (oracle/, FP64, all host threads) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO / "nematic-worms_gb300"))
+
+GAP = 10
+PEAKS_FILE = REPO / "MEASURED_PEAKS.json"
+TRAFFIC_FILE = REPO / "profiles" / "traffic_per_unit.txt"
+FALLBACK_HBM_GBS = 6800.0
+
+WORKLOADS = {
+    "wca_srd_400k": dict(k=1, layout="patches"),
+    "wca_dense_2m": dict(k=2, layout="rows"),
+    "wca_small_4k": dict(k=0, layout="patches"),
+}
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+# ---- algorithmic bytes per launch (reference float4 state model) -------------------
+def alg_bytes(name: str, cfg) -> float:
+    """Compulsory DRAM bytes of one launch of kernel `name`: every input read
+    once, every output written once, in the reference's float4 layout."""
+    nb, nt = cfg.n_beads, cfg.n_beads + cfg.n_solvent
+    C, Cs = cfg.n_cells, cfg.n_srd_cells
+    ns = cfg.n_solvent
+    table = {
+        # r, v, f, f_old read (64 B); r, v, f_old, f, tangent written (80 B); hash + slot (8 B)
+        "filament_pass": 152.0 * nb,
+        # count read, offset/start/end written, count reset
+        "scan_cells": 20.0 * C,
+        "srd_scan_cells": 20.0 * Cs,
+        # hash + slot read, index written
+        "scatter": 12.0 * nb,
+        "srd_scatter": 12.0 * nt,
+        # bucket index + hash + position read; sorted index, hash, position written
+        "stable_gather": 48.0 * nb,
+        # sorted position + index read, force read-modify-write, cell bounds read
+        "pair_wca": 52.0 * nb + 8.0 * C,
+        "pair_ref": 84.0 * nb + 8.0 * C,
+        # position read, hash + slot written
+        "srd_hash": 24.0 * nt,
+        # member index + velocity read/write; solvent position read/write; cell offsets + mean
+        "srd_collide": 36.0 * nt + 32.0 * ns + 20.0 * Cs,
+        "advance_step": 8.0,
+    }
+    return table.get(name, 0.0)
+
+
+def read_peak():
+    try:
+        d = json.loads(PEAKS_FILE.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def read_traffic(name: str):
+    """DRAM bytes per unit of work of a kernel from the committed ncu summary."""
+    try:
+        for line in TRAFFIC_FILE.read_text().splitlines():
+            parts = line.split()
+            if len(parts) >= 3 and parts[0] == name and not line.startswith("#"):
+                return float(parts[1]), parts[2]
+    except Exception:
+        pass
+    return None
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"nw_clocks_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = max(mx, float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        self.path.unlink(missing_ok=True)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(cfg, pos, vel, budget_s: float = 20.0):
+    """FP64 CPU port of the step (oracle/, OpenMP over all host threads) on a
+    bounded sample of the same workload: whole bead steps without SRD plus
+    one SRD collision, combined as t_bead + t_srd / gap."""
+    sys.path.insert(0, str(REPO / "oracle"))
+    import numpy as np
+
+    import oracle as orc
+
+    orc.set_threads(os.cpu_count() or 1)
+    nb = cfg.n_beads
+    c_beads = cfg.copy()
+    c_beads.srd_enabled = 0
+    z = np.zeros((nb, 4), np.float64)
+    st = dict(pos=pos[:nb], vel=vel[:nb], force=z, force_old=z, tangent=z)
+    t0 = time.perf_counter()
+    n_bead = 0
+    while True:
+        st = orc.step(c_beads, st, n_bead, cfg.dt, 64)
+        n_bead += 1
+        if time.perf_counter() - t0 > budget_s * 0.5 or n_bead >= 20:
+            break
+    t_bead = (time.perf_counter() - t0) / n_bead
+    t_srd = 0.0
+    if cfg.srd_enabled:
+        t1 = time.perf_counter()
+        orc.srd(cfg, pos, vel, nb, cfg.n_solvent, orc.srd_shift(cfg, 0, 64), None, 0, cfg.dt * cfg.srd_gap, 64)
+        t_srd = time.perf_counter() - t1
+    per_step = t_bead + t_srd / max(1, cfg.srd_gap)
+    sample = f"{n_bead} full bead steps ({nb} beads, FP64)" + (
+        f" + 1 SRD collision ({nb + cfg.n_solvent} particles), per step = bead + SRD/{cfg.srd_gap}" if cfg.srd_enabled else "")
+    return {"value": nb / per_step, "unit": "bead-steps/s", "cores": orc.num_threads(), "kind": "port",
+            "sample": sample, "seconds_per_step": per_step}
+
+
+def workload_config(name: str, seed: int):
+    from nwgb.init import baseline_config, initial_state
+
+    w = WORKLOADS[name]
+    cfg = baseline_config(w["k"], seed=seed)
+    pos, vel = initial_state(cfg, seed=seed, layout=w["layout"])
+    return cfg, pos, vel
+
+
+def config_block(name, cfg, world):
+    return {"workload": name, "filaments": int(cfg.num_filaments), "filament_size": int(cfg.filament_size),
+            "beads": cfg.n_beads, "solvent": cfg.n_solvent, "box": [float(cfg.box[0]), float(cfg.box[1])],
+            "model": "WCA_WORMS", "srd_gap": int(cfg.srd_gap) if cfg.srd_enabled else None, "dt": float(cfg.dt),
+            "global_batch": cfg.n_beads * world, "parallelism": f"replicas x{world}",
+            "l2": "state larger than L2 (no flush needed)"}
+
+
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    import numpy as np
+
+    cfg, pos, vel = workload_config(args.workload, 0)
+    sys.path.insert(0, str(REPO / "oracle"))
+    import oracle as orc
+
+    orc.set_threads(os.cpu_count() or 1)
+    nb = cfg.n_beads
+    z = np.zeros((nb, 4), np.float64)
+    st = dict(pos=pos.astype(np.float64), vel=vel.astype(np.float64), force=z, force_old=z, tangent=z)
+    # each step of this arm is one full step of the workload on the host cores;
+    # timed steps cover whole SRD periods (the collision every srd_gap steps
+    # is part of the per-step cost) and the run is capped to a few minutes
+    period = int(cfg.srd_gap) if cfg.srd_enabled else 1
+    t_w = time.perf_counter()
+    for s in range(period):
+        st = orc.step(cfg, st, s, cfg.dt, 64)
+    per_period = max(1e-3, time.perf_counter() - t_w)
+    periods = max(1, min(-(-args.steps // period), int(120.0 / per_period)))
+    n = periods * period
+    t0 = time.perf_counter()
+    for s in range(n):
+        st = orc.step(cfg, st, period + s, cfg.dt, 64)
+    dt = time.perf_counter() - t0
+    value = nb * n / dt
+    line = {"metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": world, "steps": n,
+            "warmup": period, "ms_per_step": 1e3 * dt / n, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": config_block(args.workload, cfg, 1),
+            "cpu_baseline": {"value": value, "unit": "bead-steps/s", "cores": orc.num_threads(), "kind": "port",
+                             "sample": f"{n} full steps of the workload (FP64 port of the reference step; "
+                                       f"{args.steps} requested, capped at ~2 min)"},
+            "e2e": {"value": value, "unit": "bead-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import nwgb
+    from nwgb import abi
+
+    rank, world, local = env_rank()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    cfg, pos, vel = workload_config(args.workload, seed=rank)
+    nb = cfg.n_beads
+    sysm = nwgb.System(cfg)
+    stream = torch.cuda.current_stream()
+    sysm.set_stream(stream.cuda_stream)
+    sysm.set_array(abi.NW_POSITION, pos)
+    sysm.set_array(abi.NW_VELOCITY, vel)
+    sysm.zero_forces()
+
+    chunk = GAP if cfg.srd_enabled else 10
+    rem = args.steps % chunk
+    sched = [chunk] * (args.steps // chunk) + ([rem] if rem else [])
+    # warm-up: at least W steps in whole SRD periods, which captures the
+    # 10-step graph; a remainder graph is captured here as well
+    warm = 0
+    while warm < args.warmup:
+        sysm.step(chunk, cfg.dt)
+        warm += chunk
+    if rem:
+        sysm.step(rem, cfg.dt)
+        sysm.step(chunk - rem, cfg.dt)
+        warm += chunk
+    sysm.sync()
+
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)  # let the sampler start before the timed region
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    gpu_launches = 0
+    ev0.record(stream)
+    for n in sched:
+        sysm.step(n, cfg.dt)
+        gpu_launches += sysm.last_launch_count
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    if dist:
+        dist.barrier()
+    sysm.sync()
+    ms_t = torch.tensor([ms], device="cuda")
+    if dist:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms_max = float(ms_t.item())
+    value = nb * args.steps * world / (ms_max / 1e3)
+
+    # ---- end to end through the C ABI with host buffers ------------------------------
+    e2e_steps = max(chunk, min(200, args.steps))
+    hp = torch.empty((nb, 4), dtype=torch.float32, pin_memory=True).numpy()
+    hv = torch.empty((nb, 4), dtype=torch.float32, pin_memory=True).numpy()
+    hp[:] = sysm.get_array(abi.NW_POSITION, 0, nb)
+    hv[:] = sysm.get_array(abi.NW_VELOCITY, 0, nb)
+    sysm.set_graphs(False)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sysm.set_array(abi.NW_POSITION, hp, 0)
+        sysm.set_array(abi.NW_VELOCITY, hv, 0)
+        sysm.step(1, cfg.dt)
+        hp[:] = sysm.get_array(abi.NW_POSITION, 0, nb)
+        hv[:] = sysm.get_array(abi.NW_VELOCITY, 0, nb)
+    e2e_s = time.perf_counter() - t0
+    e2e_t = torch.tensor([e2e_s], device="cuda")
+    if dist:
+        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+    e2e_value = nb * e2e_steps * world / float(e2e_t.item())
+    sysm.set_graphs(True)
+
+    # ---- per-kernel device time (events around every launch) ---------------------------
+    prof = sysm.profile(2 * chunk, cfg.dt)
+    sysm.sync()
+    dom = max((k for k in prof if k != "advance_step"), key=lambda k: prof[k][0])
+    dom_ms = prof[dom][0] / prof[dom][1]
+    peak, peak_kind = read_peak()
+    bytes_launch = alg_bytes(dom, cfg)
+    achieved = bytes_launch / (dom_ms / 1e3) / 1e9
+    tr = read_traffic(dom)
+    traffic = None
+    if tr is not None:
+        per_unit, unit = tr
+        units = {"bead": nb, "particle": nb + cfg.n_solvent, "cell": cfg.n_cells, "srd_cell": cfg.n_srd_cells}.get(unit)
+        traffic = per_unit * units if units else None
+    total_prof = sum(v[0] for v in prof.values())
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
+                "traffic": traffic, "alg_bytes_per_launch": bytes_launch, "avg_launch_ms": dom_ms,
+                "kernel_share": {k: round(v[0] / total_prof, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}}
+
+    if rank == 0:
+        line = {"metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": warm, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": config_block(args.workload, cfg, world), "clocks": clk,
+                "e2e": {"value": e2e_value, "unit": "bead-steps/s", "h2d_bytes_per_step": nb * 32,
+                        "d2h_bytes_per_step": nb * 32, "steps": e2e_steps,
+                        "path": "nw_set_array(pos, vel) + nw_step(1) + nw_get_array(pos, vel) per step, pinned host"},
+                "gpu_launches": gpu_launches, "roofline": roofline}
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(cfg, pos.astype(np.float64), vel.astype(np.float64))
+        print(json.dumps(line), flush=True)
+    sysm.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20000)
+    ap.add_argument("--warmup", type=int, default=100)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="wca_srd_400k")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -253,6 +253,17 @@ size_t nw_config_size(void);
  * kernels inside the graph). */
 nw_status nw_last_launch_count(const nw_system* sys, uint64_t* launches);
 
+/* Per-kernel device time of `nsteps` steps (direct launches, a CUDA event
+ * before every kernel), aggregated by kernel name.  Advances the system like
+ * nw_step.  Replaces the reference's host-clock phase counters
+ * (archived/vs_solution/fluid_substrate/NWWorms.h:637-654). */
+typedef struct NwKernelTime {
+    char name[32];
+    double total_ms;
+    uint64_t launches;
+} NwKernelTime;
+nw_status nw_profile_steps(nw_system* sys, int nsteps, float dt, NwKernelTime* out, int max_entries, int* n_entries);
+
 #ifdef __cplusplus
 }
 #endif

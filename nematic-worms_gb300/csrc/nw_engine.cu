@@ -76,38 +76,77 @@ static uint32_t filaments_per_block(uint32_t L, uint32_t nf)
     return fpb ? fpb : 1u;
 }
 
+void Prof::mark(const char* name)
+{
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, stream);
+    events.push_back(e);
+    names.emplace_back(name);
+}
+
+void Prof::end()
+{
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, stream);
+    events.push_back(e);
+    names.emplace_back("");
+}
+
+void Prof::clear()
+{
+    for (auto e : events) cudaEventDestroy(e);
+    events.clear();
+    names.clear();
+}
+
+#define NW_MARK(name) \
+    if (prof) prof->mark(name)
+
 uint64_t enqueue_bead_step(const DevParams& P, const StepBuffers& B, uint32_t nchunks, uint32_t step_off, float dt,
-                           cudaStream_t s)
+                           cudaStream_t s, Prof* prof)
 {
     if (P.nb == 0) return 0;
     const uint32_t fpb = filaments_per_block(P.L, P.nf);
     const uint32_t beads = fpb * P.L;
     const uint32_t threads = (beads + 31u) & ~31u;
     const size_t smem = (size_t)beads * sizeof(float4) * (P.reverse_on ? 3u : 1u);
+    NW_MARK("filament_pass");
     filament_pass_kernel<<<cdiv(P.nf, fpb), threads, smem, s>>>(P, B, step_off, dt, fpb);
+    NW_MARK("scan_cells");
     scan_cells_kernel<true><<<nchunks, 512, 0, s>>>(B.cell_count, B.chunk_count, P.ncells, B.cell_offset, B.cell_start,
                                                     B.cell_end);
+    NW_MARK("scatter");
     scatter_kernel<<<cdiv(P.nb, 256), 256, 0, s>>>(B.hash, B.slot, B.cell_offset, B.tmp_index, P.nb, B.chunk_count,
                                                    nchunks);
     if (P.model == NW_MODEL_REF_DEM) {
+        NW_MARK("stable_gather");
         stable_gather_kernel<true><<<cdiv(P.nb, 256), 256, 0, s>>>(P, B);
+        NW_MARK("pair_ref");
         pair_ref_kernel<<<cdiv(P.nb, 256), 256, 0, s>>>(P, B);
     } else {
+        NW_MARK("stable_gather");
         stable_gather_kernel<false><<<cdiv(P.nb, 256), 256, 0, s>>>(P, B);
+        NW_MARK("pair_wca");
         pair_wca_kernel<<<cdiv(P.nb, 256), 256, 0, s>>>(P, B);
     }
     return 5;
 }
 
 uint64_t enqueue_srd(const DevParams& P, const StepBuffers& B, uint32_t srd_nchunks, uint32_t step_off, float dt_srd,
-                     int shift_from_step, float3 shift, cudaStream_t s)
+                     int shift_from_step, float3 shift, cudaStream_t s, Prof* prof)
 {
     if (P.ntotal == 0) return 0;
+    NW_MARK("srd_hash");
     srd_hash_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(P, B, step_off, shift_from_step, shift);
+    NW_MARK("srd_scan_cells");
     scan_cells_kernel<true><<<srd_nchunks, 512, 0, s>>>(B.srd_count, B.srd_chunk, P.srd_ncells, B.srd_offset,
                                                         B.srd_start, B.srd_end);
+    NW_MARK("srd_scatter");
     scatter_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(B.srd_hash, B.srd_slot, B.srd_offset, B.srd_tmp, P.ntotal,
                                                        B.srd_chunk, srd_nchunks);
+    NW_MARK("srd_collide");
     srd_collide_kernel<<<cdiv(P.srd_ncells, 256), 256, 0, s>>>(P, B, step_off, dt_srd);
     return 4;
 }
@@ -205,18 +244,20 @@ ArrayInfo array_info(nw_system* s, int array)
 }
 
 // Enqueue `nsteps` steps starting at device step base + 0 and advance the base.
-uint64_t enqueue_steps(nw_system* s, int nsteps, float dt, uint64_t first_step)
+uint64_t enqueue_steps(nw_system* s, int nsteps, float dt, uint64_t first_step, Prof* prof = nullptr)
 {
     const DevParams P = make_dev_params(s->cfg, dt);
     uint64_t launches = 0;
     for (int j = 0; j < nsteps; ++j) {
-        launches += enqueue_bead_step(P, s->B, s->nchunks, (uint32_t)j, dt, s->stream);
+        launches += enqueue_bead_step(P, s->B, s->nchunks, (uint32_t)j, dt, s->stream, prof);
         const uint64_t st = first_step + (uint64_t)j;
         if (s->cfg.srd_enabled && (st % s->cfg.srd_gap) == 0)
             launches += enqueue_srd(P, s->B, s->srd_nchunks, (uint32_t)j, dt * (float)s->cfg.srd_gap, 1,
-                                    make_float3(0.f, 0.f, 0.f), s->stream);
+                                    make_float3(0.f, 0.f, 0.f), s->stream, prof);
     }
+    if (prof) prof->mark("advance_step");
     advance_step_kernel<<<1, 1, 0, s->stream>>>(s->B.step_base, (unsigned long long)nsteps);
+    if (prof) prof->end();
     return launches + 1;
 }
 
@@ -614,6 +655,41 @@ nw_status nw_last_launch_count(const nw_system* s, uint64_t* launches)
 {
     if (!s || !launches) return NW_ERR_INVALID;
     *launches = s->last_launches;
+    return NW_OK;
+}
+
+nw_status nw_profile_steps(nw_system* s, int nsteps, float dt, NwKernelTime* out, int max_entries, int* n_entries)
+{
+    if (!s || nsteps < 1 || !out || max_entries < 1 || !n_entries) return NW_ERR_INVALID;
+    if (!(dt > 0.0f)) dt = s->cfg.dt;
+    Prof prof;
+    prof.stream = s->stream;
+    s->last_launches = enqueue_steps(s, nsteps, dt, s->step, &prof);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) {
+        prof.clear();
+        return cuda_status(e);
+    }
+    s->step += (uint64_t)nsteps;
+    int n = 0;
+    for (size_t k = 0; k + 1 < prof.events.size(); ++k) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, prof.events[k], prof.events[k + 1]);
+        int slot = -1;
+        for (int q = 0; q < n; ++q)
+            if (std::strncmp(out[q].name, prof.names[k].c_str(), sizeof(out[q].name)) == 0) slot = q;
+        if (slot < 0) {
+            if (n >= max_entries) continue;
+            slot = n++;
+            std::memset(&out[slot], 0, sizeof(out[slot]));
+            std::strncpy(out[slot].name, prof.names[k].c_str(), sizeof(out[slot].name) - 1);
+        }
+        out[slot].total_ms += ms;
+        out[slot].launches += 1;
+    }
+    *n_entries = n;
+    prof.clear();
     return NW_OK;
 }
 

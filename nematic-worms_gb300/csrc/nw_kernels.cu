@@ -126,6 +126,10 @@ __global__ void __launch_bounds__(256) pair_ref_kernel(const DevParams P, const 
     const float3 t = f3(S.sorted_tan[p]);
     const int3 g = grid_pos(P, r);
     const uint32_t me = S.sorted_index[p];
+    if (me >= P.nb) {
+        atomicOr(S.err, (uint32_t)NW_EFLAG_BAD_INDEX);
+        return;
+    }
     const uint32_t fI = me / P.L, cI = me - fI * P.L;
     float3 total = zero3();
     if (P.grid[2] == 1u) {
@@ -169,6 +173,10 @@ __global__ void __launch_bounds__(256) pair_wca_kernel(const DevParams P, const 
     const int ny = axis_cells(P, 1, cell_coord(P, 1, g.y), cy);
     const int nz = axis_cells(P, 2, cell_coord(P, 2, g.z), cz);
     const uint32_t me = S.sorted_index[p];
+    if (me >= P.nb) {
+        atomicOr(S.err, (uint32_t)NW_EFLAG_BAD_INDEX);
+        return;
+    }
     const uint32_t fI = me / P.L;
     const int cI = (int)(me - fI * P.L);
     float3 f = zero3();
@@ -176,13 +184,8 @@ __global__ void __launch_bounds__(256) pair_wca_kernel(const DevParams P, const 
         for (int ky = 0; ky < ny; ++ky)
             for (int kx = 0; kx < nx; ++kx) {
                 const uint32_t h = (cz[kz] * P.grid[1] + cy[ky]) * P.grid[0] + cx[kx];
-                const uint32_t s0 = __ldg(&S.cell_start[h]);
-                if (s0 == kEmpty) continue;
-                uint32_t s1 = __ldg(&S.cell_end[h]);
-                if (s1 - s0 > kPairCap) {
-                    atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
-                    s1 = s0 + kPairCap;
-                }
+                uint32_t s0, s1;
+                if (!cell_range(P, S, h, s0, s1)) continue;
                 for (uint32_t j = s0; j < s1; ++j) {
                     if (j == p) continue;
                     const uint32_t o = __ldg(&S.sorted_index[j]);

@@ -262,18 +262,32 @@ __global__ void __launch_bounds__(256) stable_gather_kernel(const DevParams P, c
 
 // ---- K5: pair forces ---------------------------------------------------------------
 
+// Member range [s0, s1) of cell h, checked against the particle count (cell
+// bounds handed in through the legacy C ABI are caller data); false if empty.
+__device__ __forceinline__ bool cell_range(const DevParams& P, const StepBuffers& S, uint32_t h, uint32_t& s0,
+                                           uint32_t& s1)
+{
+    s0 = __ldg(&S.cell_start[h]);
+    if (s0 == kEmpty) return false;
+    s1 = __ldg(&S.cell_end[h]);
+    if (s0 >= P.nb || s1 > P.nb || s1 < s0) {
+        atomicOr(S.err, (uint32_t)NW_EFLAG_BAD_INDEX);
+        return false;
+    }
+    if (s1 - s0 > kPairCap) {
+        atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
+        s1 = s0 + kPairCap;
+    }
+    return true;
+}
+
 // collideCell for one neighbour cell (particles_kernel_impl.cuh:492-556).
 __device__ __forceinline__ float3 ref_cell_sum(const DevParams& P, const StepBuffers& S, uint32_t h, uint32_t p,
                                                float3 r, float3 v, float3 t, uint32_t fI, uint32_t cI)
 {
     float3 sum = zero3();
-    const uint32_t s0 = __ldg(&S.cell_start[h]);
-    if (s0 == kEmpty) return sum;
-    uint32_t s1 = __ldg(&S.cell_end[h]);
-    if (s1 - s0 > kPairCap) {
-        atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
-        s1 = s0 + kPairCap;
-    }
+    uint32_t s0, s1;
+    if (!cell_range(P, S, h, s0, s1)) return sum;
     const float cd = P.radius + P.radius;
     for (uint32_t j = s0; j < s1; ++j) {
         if (j == p) continue;

@@ -193,6 +193,10 @@ __global__ void reorder_kernel(uint32_t* cellStart, uint32_t* cellEnd, float4* s
     }
     if (i == n - 1 && h < numCells) cellEnd[h] = i + 1;
     const uint32_t s = index[i];
+    if (s >= n) {
+        atomicOr(err, (uint32_t)NW_EFLAG_BAD_INDEX);
+        return;
+    }
     sPos[i] = pos[s];
     if (vel && sVel) sVel[i] = vel[s];
     if (tan && sTan) sTan[i] = tan[s];

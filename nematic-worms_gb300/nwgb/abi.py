@@ -134,6 +134,12 @@ class NwConfig(C.Structure):
         return int(self.srd_grid[0]) * int(self.srd_grid[1]) * int(self.srd_grid[2])
 
 
+class NwKernelTime(C.Structure):
+    """Mirror of ``struct NwKernelTime`` (include/nwgb.h)."""
+
+    _fields_ = [("name", C.c_char * 32), ("total_ms", C.c_double), ("launches", C.c_uint64)]
+
+
 class NwError(RuntimeError):
     """A libnwgb call returned a non-OK nw_status."""
 
@@ -186,6 +192,7 @@ HANDLE_API = [
     ("nw_abi_version", _u32, []),
     ("nw_config_size", C.c_size_t, []),
     ("nw_last_launch_count", C.c_int, [_sysp, C.POINTER(C.c_uint64)]),
+    ("nw_profile_steps", C.c_int, [_sysp, C.c_int, _f32, C.POINTER(NwKernelTime), C.c_int, C.POINTER(C.c_int)]),
 ]
 
 _fp = C.c_void_p  # device pointers are passed as integers

@@ -130,6 +130,14 @@ class System:
         check(self.lib.nw_last_launch_count(self._h, C.byref(n)))
         return n.value
 
+    def profile(self, n: int, dt: float = 0.0) -> dict:
+        """Run n steps with a CUDA event around every kernel; returns
+        {kernel name: (total ms, launches)}."""
+        buf = (abi.NwKernelTime * 32)()
+        cnt = C.c_int()
+        check(self.lib.nw_profile_steps(self._h, int(n), float(dt), buf, 32, C.byref(cnt)), "nw_profile_steps")
+        return {buf[k].name.decode(): (buf[k].total_ms, int(buf[k].launches)) for k in range(cnt.value)}
+
     # -- checkpoints ------------------------------------------------------------------------
     def checkpoint(self) -> bytes:
         n = C.c_size_t()

@@ -94,10 +94,13 @@ def test_legacy_bead_pipeline_matches_reference(lib, name):
     assert np.array_equal(host(sp), d["sorted_pos"])
     # DEM contact + cell-list bond + extensile drive
     f = torch_dev(d["fil_force"])
-    lib.collideFilaments(ptr(f), ptr(torch_dev(d["sorted_pos"])), ptr(torch_dev(d["sorted_vel"])),
-                         ptr(torch_dev(d["sorted_tan"])), ptr(torch_dev(d["sorted_index"].view(np.int32))),
-                         ptr(torch_dev(d["cell_start"].view(np.int32))), ptr(torch_dev(d["cell_end"].view(np.int32))),
-                         nb, ncell)
+    # every device buffer stays referenced until the kernel has run
+    bufs = [torch_dev(d["sorted_pos"]), torch_dev(d["sorted_vel"]), torch_dev(d["sorted_tan"]),
+            torch_dev(d["sorted_index"].view(np.int32)), torch_dev(d["cell_start"].view(np.int32)),
+            torch_dev(d["cell_end"].view(np.int32))]
+    lib.collideFilaments(ptr(f), *[ptr(b) for b in bufs], nb, ncell)
+    torch.cuda.synchronize()
+    del bufs
     assert rel_err(host(f), d["collide_force"]) < TOL
     assert lib.nw_legacy_last_status() == 0
 
@@ -108,7 +111,8 @@ def test_legacy_reverse_matches_reference(lib):
     c2.reverse_probability = 0.3
     set_legacy_params(lib, c2)
     f, fo, v, p = (torch_dev(d[k]) for k in ("int_force", "int_force_old", "int_vel", "int_pos"))
-    lib.nw_legacy_reverse_apply(ptr(f), ptr(fo), ptr(v), ptr(p), ptr(torch_dev(d["uniform"])), cfg.num_filaments)
+    uni = torch_dev(d["uniform"])
+    lib.nw_legacy_reverse_apply(ptr(f), ptr(fo), ptr(v), ptr(p), ptr(uni), cfg.num_filaments)
     for t, k in ((p, "rev_pos"), (v, "rev_vel"), (f, "rev_force"), (fo, "rev_force_old")):
         assert np.array_equal(host(t), d[k]), k
 
@@ -140,7 +144,8 @@ def test_legacy_srd_pipeline_matches_reference(lib):
     com = torch.zeros((nsc, 4), dtype=torch.float32, device="cuda")
     lib.solventCellCentorOfMomentum(ptr(com), ptr(sv), ptr(cs), ptr(ce), ptr(ix), nsc)
     assert rel_err(host(com), d["com"]) < TOL
-    lib.nw_legacy_collide_solvent_apply(ptr(p), ptr(v), ptr(com), ptr(torch_dev(d["uniform"])), n)
+    uni = torch_dev(d["uniform"])
+    lib.nw_legacy_collide_solvent_apply(ptr(p), ptr(v), ptr(com), ptr(uni), n)
     assert rel_err(host(v), d["coll_vel"]) < TOL
     lib.integrateSolvent(ptr(p), ptr(v), float(d["dt_srd"]), cfg.n_beads, cfg.n_solvent)
     assert rel_err(host(p), d["pos_out"]) < TOL and rel_err(host(v), d["vel_out"]) < TOL
