@@ -254,7 +254,10 @@ def run_ours(args):
     cfg, pos, vel = workload_config(args.workload, seed=rank)
     nb = cfg.n_beads
     sysm = nwgb.System(cfg)
-    stream = torch.cuda.current_stream()
+    # the engine runs on a dedicated (non-default) stream that the CUDA events
+    # below are recorded on
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sysm.set_stream(stream.cuda_stream)
     sysm.set_array(abi.NW_POSITION, pos)
     sysm.set_array(abi.NW_VELOCITY, vel)
@@ -315,8 +318,8 @@ def run_ours(args):
         sysm.set_array(abi.NW_POSITION, hp, 0)
         sysm.set_array(abi.NW_VELOCITY, hv, 0)
         sysm.step(1, cfg.dt)
-        hp[:] = sysm.get_array(abi.NW_POSITION, 0, nb)
-        hv[:] = sysm.get_array(abi.NW_VELOCITY, 0, nb)
+        sysm.get_array(abi.NW_POSITION, 0, nb, out=hp)
+        sysm.get_array(abi.NW_VELOCITY, 0, nb, out=hv)
     e2e_s = time.perf_counter() - t0
     e2e_t = torch.tensor([e2e_s], device="cuda")
     if dist:

@@ -114,12 +114,13 @@ uint64_t enqueue_bead_step(const DevParams& P, const StepBuffers& B, uint32_t nc
     const size_t smem = (size_t)beads * sizeof(float4) * (P.reverse_on ? 3u : 1u);
     NW_MARK("filament_pass");
     filament_pass_kernel<<<cdiv(P.nf, fpb), threads, smem, s>>>(P, B, step_off, dt, fpb);
+    NW_MARK("chunk_sum");
+    chunk_sum_kernel<<<nchunks, 512, 0, s>>>(B.cell_count, P.ncells, B.chunk_count);
     NW_MARK("scan_cells");
     scan_cells_kernel<true><<<nchunks, 512, 0, s>>>(B.cell_count, B.chunk_count, P.ncells, B.cell_offset, B.cell_start,
                                                     B.cell_end);
     NW_MARK("scatter");
-    scatter_kernel<<<cdiv(P.nb, 256), 256, 0, s>>>(B.hash, B.slot, B.cell_offset, B.tmp_index, P.nb, B.chunk_count,
-                                                   nchunks);
+    scatter_kernel<<<cdiv(P.nb, 256), 256, 0, s>>>(B.hash, B.slot, B.cell_offset, B.tmp_index, P.nb);
     if (P.model == NW_MODEL_REF_DEM) {
         NW_MARK("stable_gather");
         stable_gather_kernel<true><<<cdiv(P.nb, 256), 256, 0, s>>>(P, B);
@@ -131,7 +132,7 @@ uint64_t enqueue_bead_step(const DevParams& P, const StepBuffers& B, uint32_t nc
         NW_MARK("pair_wca");
         pair_wca_kernel<<<cdiv(P.nb, 256), 256, 0, s>>>(P, B);
     }
-    return 5;
+    return 6;
 }
 
 uint64_t enqueue_srd(const DevParams& P, const StepBuffers& B, uint32_t srd_nchunks, uint32_t step_off, float dt_srd,
@@ -140,15 +141,16 @@ uint64_t enqueue_srd(const DevParams& P, const StepBuffers& B, uint32_t srd_nchu
     if (P.ntotal == 0) return 0;
     NW_MARK("srd_hash");
     srd_hash_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(P, B, step_off, shift_from_step, shift);
+    NW_MARK("srd_chunk_sum");
+    chunk_sum_kernel<<<srd_nchunks, 512, 0, s>>>(B.srd_count, P.srd_ncells, B.srd_chunk);
     NW_MARK("srd_scan_cells");
     scan_cells_kernel<true><<<srd_nchunks, 512, 0, s>>>(B.srd_count, B.srd_chunk, P.srd_ncells, B.srd_offset,
                                                         B.srd_start, B.srd_end);
     NW_MARK("srd_scatter");
-    scatter_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(B.srd_hash, B.srd_slot, B.srd_offset, B.srd_tmp, P.ntotal,
-                                                       B.srd_chunk, srd_nchunks);
+    scatter_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(B.srd_hash, B.srd_slot, B.srd_offset, B.srd_tmp, P.ntotal);
     NW_MARK("srd_collide");
     srd_collide_kernel<<<cdiv(P.srd_ncells, 256), 256, 0, s>>>(P, B, step_off, dt_srd);
-    return 4;
+    return 5;
 }
 
 }  // namespace nw

@@ -103,16 +103,40 @@ __global__ void __launch_bounds__(1024) filament_pass_kernel(const DevParams P, 
 
     const uint32_t h = bead_hash(P, f3(nP));
     S.hash[i] = h;
-    S.slot[i] = count_into_cell(S.cell_count, S.chunk_count, h);
+    S.slot[i] = count_into_cell(S.cell_count, h);
+}
+
+__global__ void __launch_bounds__(512) chunk_sum_kernel(const uint32_t* __restrict__ a, uint32_t m,
+                                                        uint32_t* __restrict__ chunk)
+{
+    __shared__ uint32_t s_w[16];
+    const uint32_t c0 = blockIdx.x * kChunk;
+    uint32_t x = 0;
+    if (c0 + kChunk <= m) {
+        const uint4* v = reinterpret_cast<const uint4*>(a + c0);
+        for (uint32_t k = threadIdx.x; k < kChunk / 4u; k += 512u) {
+            const uint4 q = v[k];
+            x += q.x + q.y + q.z + q.w;
+        }
+    } else {
+        for (uint32_t k = threadIdx.x; k < kChunk; k += 512u)
+            if (c0 + k < m) x += a[c0 + k];
+    }
+    x = warp_sum(x);
+    if ((threadIdx.x & 31u) == 0) s_w[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint32_t y = threadIdx.x < 16 ? s_w[threadIdx.x] : 0u;
+        y = warp_sum(y);
+        if (threadIdx.x == 0) chunk[blockIdx.x] = y;
+    }
 }
 
 __global__ void __launch_bounds__(256) scatter_kernel(const uint32_t* __restrict__ hash,
                                                       const uint32_t* __restrict__ slot,
                                                       const uint32_t* __restrict__ offset, uint32_t* __restrict__ tmp,
-                                                      uint32_t n, uint32_t* __restrict__ chunk_count, uint32_t nchunks)
+                                                      uint32_t n)
 {
-    if (blockIdx.x == 0)
-        for (uint32_t k = threadIdx.x; k < nchunks; k += blockDim.x) chunk_count[k] = 0u;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) tmp[offset[hash[i]] + slot[i]] = i;
 }
@@ -222,7 +246,7 @@ __global__ void __launch_bounds__(256) srd_hash_kernel(const DevParams P, const 
     if (shift_from_step) shift = srd_shift_of(P, *S.step_base + step_off);
     const uint32_t h = srd_hash(P, f3(S.pos[i]), shift);
     S.srd_hash[i] = h;
-    S.srd_slot[i] = count_into_cell(S.srd_count, S.srd_chunk, h);
+    S.srd_slot[i] = count_into_cell(S.srd_count, h);
 }
 
 __global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,

@@ -54,15 +54,11 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x)
     return x;
 }
 
-// Count one element into its cell and, warp-aggregated, into its chunk.
-__device__ __forceinline__ uint32_t count_into_cell(uint32_t* cell_count, uint32_t* chunk_count, uint32_t h)
+// Count one element into its cell; the returned slot orders the cell's
+// members arbitrarily (the stable order is restored when the bucket is read).
+__device__ __forceinline__ uint32_t count_into_cell(uint32_t* cell_count, uint32_t h)
 {
-    const uint32_t slot = atomicAdd(&cell_count[h], 1u);
-    const uint32_t ck = h >> kChunkLog2;
-    const uint32_t am = __activemask();
-    const uint32_t peers = __match_any_sync(am, ck);
-    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&chunk_count[ck], (uint32_t)__popc(peers));
-    return slot;
+    return atomicAdd(&cell_count[h], 1u);
 }
 
 // ---- bonded helpers ----------------------------------------------------------
@@ -127,8 +123,8 @@ __global__ void __launch_bounds__(1024) filament_pass_kernel(const DevParams P, 
                                                              float dt, uint32_t fpb);
 
 // ---- K2: cell scan ---------------------------------------------------------------
-// Block b scans cells [b*4096, (b+1)*4096); the counts of all earlier chunks
-// were accumulated by the producer, so no block waits on another.
+// Block b scans cells [b*4096, (b+1)*4096); the totals of all earlier chunks
+// come from chunk_sum_kernel, so no block waits on another.
 // offset[c] = exclusive prefix, offset[ncells] = total; start/end in the
 // reference's format (0xffffffff for empty cells); counts are reset to zero.
 template <bool kBounds>
@@ -219,11 +215,16 @@ __global__ void __launch_bounds__(512) scan_cells_kernel(uint32_t* __restrict__ 
     if (c0 < ncells && c0 + 8u >= ncells) offset[ncells] = run;
 }
 
+// Sum of each 4096-entry chunk of the cell counts (feeds scan_cells_kernel,
+// whose blocks then need no communication with one another).
+__global__ void __launch_bounds__(512) chunk_sum_kernel(const uint32_t* __restrict__ a, uint32_t m,
+                                                        uint32_t* __restrict__ chunk);
+
 // ---- K3: scatter into cell buckets (arbitrary order inside a bucket) -------------
 __global__ void __launch_bounds__(256) scatter_kernel(const uint32_t* __restrict__ hash,
                                                       const uint32_t* __restrict__ slot,
                                                       const uint32_t* __restrict__ offset, uint32_t* __restrict__ tmp,
-                                                      uint32_t n, uint32_t* __restrict__ chunk_count, uint32_t nchunks);
+                                                      uint32_t n);
 
 // Rank of element `i` among the members of its bucket (= stable position).
 __device__ __forceinline__ uint32_t bucket_rank(const uint32_t* __restrict__ tmp, uint32_t lo, uint32_t hi, uint32_t i,

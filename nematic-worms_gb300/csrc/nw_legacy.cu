@@ -505,20 +505,13 @@ void sortParticles(uint* dGridParticleHash, uint* dGridParticleIndex, uint numPa
     if (g_radix.capacity < numParticles) {
         cudaFree(g_radix.keys_alt);
         g_radix = RadixScratch();
-        size_t hw = 0, cw = 0;
-        radix_scratch_words(numParticles, &hw, &cw);
         uint32_t* base = nullptr;
-        const size_t words = 2 * (size_t)numParticles + 2 * hw + cw;
+        const size_t words = radix_scratch_layout(numParticles, nullptr, nullptr);
         if (cudaMalloc(&base, words * sizeof(uint32_t)) != cudaSuccess) {
             note(cudaErrorMemoryAllocation, "sortParticles");
             return;
         }
-        g_radix.keys_alt = base;
-        g_radix.vals_alt = base + numParticles;
-        g_radix.ghist = base + 2 * (size_t)numParticles;
-        g_radix.goffset = g_radix.ghist + hw;
-        g_radix.chunk = g_radix.goffset + hw;
-        g_radix.capacity = numParticles;
+        radix_scratch_layout(numParticles, base, &g_radix);
     }
     radix_sort_pairs(dGridParticleHash, dGridParticleIndex, numParticles, g_radix, 0);
     check_launch("sortParticles");

@@ -30,25 +30,6 @@ __global__ void __launch_bounds__(256) radix_hist_kernel(const uint32_t* __restr
     ghist[threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
 }
 
-// Sum of each 4096-entry chunk of an array (feeds scan_cells_kernel).
-__global__ void __launch_bounds__(512) chunk_sum_kernel(const uint32_t* __restrict__ a, uint32_t m,
-                                                        uint32_t* __restrict__ chunk)
-{
-    __shared__ uint32_t s_w[16];
-    const uint32_t c0 = blockIdx.x * kChunk;
-    uint32_t x = 0;
-    for (uint32_t k = threadIdx.x; k < kChunk; k += 512u)
-        if (c0 + k < m) x += a[c0 + k];
-    x = warp_sum(x);
-    if ((threadIdx.x & 31u) == 0) s_w[threadIdx.x >> 5] = x;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        uint32_t y = threadIdx.x < 16 ? s_w[threadIdx.x] : 0u;
-        y = warp_sum(y);
-        if (threadIdx.x == 0) chunk[blockIdx.x] = y;
-    }
-}
-
 // Stable scatter of one tile: rounds of 256 consecutive keys; inside a round
 // the rank of a key among equal digits is (earlier warps' counts) + (earlier
 // lanes of its warp), so input order is kept.
@@ -106,14 +87,27 @@ struct RadixScratch {
     uint32_t capacity = 0;
 };
 
-// Bytes of scratch a sort of n keys needs, split as RadixScratch uses them.
-inline size_t radix_scratch_words(uint32_t n, size_t* hist_words, size_t* chunk_words)
+// Carve the scratch of a sort of up to n keys out of one buffer of 32-bit
+// words.  Every sub-array starts on a 256-byte boundary (the scan reads and
+// writes 16-byte vectors).  Returns the words needed; with base == nullptr
+// only the size is computed.
+inline size_t radix_scratch_layout(uint32_t n, uint32_t* base, RadixScratch* out)
 {
+    auto up = [](size_t w) { return (w + 63) & ~size_t(63); };
     const size_t nblocks = (n + kRadixTile - 1) / kRadixTile;
     const size_t m = 256 * (nblocks ? nblocks : 1);
-    *hist_words = m + 8;
-    *chunk_words = (m + kChunk - 1) / kChunk + 1;
-    return 2 * (size_t)n + 2 * (*hist_words) + (*chunk_words);
+    const size_t hist = up(m + 8);
+    const size_t chunk = up((m + kChunk - 1) / kChunk + 1);
+    const size_t keys = up(n ? n : 1);
+    if (base && out) {
+        out->keys_alt = base;
+        out->vals_alt = base + keys;
+        out->ghist = base + 2 * keys;
+        out->goffset = out->ghist + hist;
+        out->chunk = out->goffset + hist;
+        out->capacity = n;
+    }
+    return 2 * keys + 2 * hist + chunk;
 }
 
 // Sort (keys, vals) in place, stable, 4 passes; scratch must hold n keys.

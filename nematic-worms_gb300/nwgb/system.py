@@ -75,13 +75,20 @@ class System:
             a = np.ascontiguousarray(np.asarray(data, dtype=np.uint32).reshape(-1))
         check(self.lib.nw_set_array(self._h, which, a.ctypes.data, start, a.shape[0]), "nw_set_array")
 
-    def get_array(self, which: int, start: int = 0, count: int | None = None) -> np.ndarray:
+    def get_array(self, which: int, start: int = 0, count: int | None = None, out: np.ndarray | None = None):
+        """Copy `count` elements to host memory (a new array, or `out`, e.g. a
+        pinned buffer, which must be C-contiguous with the right dtype)."""
         if count is None:
-            count = self._size(which) - start
-        if which in _FLOAT4:
-            out = np.empty((count, 4), dtype=np.float32)
+            count = (out.shape[0] if out is not None else self._size(which) - start)
+        if out is None:
+            if which in _FLOAT4:
+                out = np.empty((count, 4), dtype=np.float32)
+            else:
+                out = np.empty(count, dtype=np.uint32)
         else:
-            out = np.empty(count, dtype=np.uint32)
+            want = np.float32 if which in _FLOAT4 else np.uint32
+            if out.dtype != want or not out.flags["C_CONTIGUOUS"] or out.shape[0] < count:
+                raise ValueError("out must be a C-contiguous array of the array's element type")
         check(self.lib.nw_get_array(self._h, which, out.ctypes.data, start, count), "nw_get_array")
         return out
 

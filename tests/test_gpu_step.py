@@ -108,9 +108,9 @@ def test_one_step_matches_oracle(lib, orc, kind):
     if cfg.srd_enabled:  # solvent after the collision of step 0
         assert rel_err(g["pos"][nb:], o["pos"][nb:]) < TOL32
         assert rel_err(g["vel"][nb:], o["vel"][nb:]) < TOL32
-        assert g["launches"] == 5 + 4 + 1
+        assert g["launches"] == 6 + 5 + 1  # bead step, SRD collision, step counter
     else:
-        assert g["launches"] == 5 + 1
+        assert g["launches"] == 6 + 1
 
 
 @pytest.mark.parametrize("kind", ["wca", "ref_srd"])
