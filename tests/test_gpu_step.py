@@ -2,8 +2,11 @@
 
 Tolerances: cell hashes, sort order and cell bounds bit-exact; positions,
 velocities and forces within 1e-5 of the FP32 oracle, measured as
-max |gpu - oracle| / max |oracle| per array; the FP64 oracle's error is
-reported alongside and bounded at 1e-4 (FP32 rounding of r^-14 terms).
+max |gpu - oracle| / max |oracle| per array.  The FP64 oracle's error is
+reported alongside and bounded at 1e-3: FP32 itself is that far from FP64 on
+the net force of beads in WCA contact (pair terms ~r^-14 that cancel; the
+FP32 oracle shows the same 1.6e-4 on the SRD case, where no Langevin noise
+sets the force scale).
 """
 from __future__ import annotations
 
@@ -17,7 +20,7 @@ from nwgb.init import initial_state, reference_reset, wca_config
 pytestmark = pytest.mark.gpu
 
 TOL32 = 1e-5
-TOL64 = 1e-4
+TOL64 = 1e-3
 
 
 def make_case(kind: str, lib):
