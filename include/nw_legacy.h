@@ -78,6 +78,19 @@ void collideSolvent(float* pos, float* vel, float* solventCellCOM, float* random
 void filamentForces(float* force, float* tangent, float* pos, float numFilaments);
 /* particleSystem_cuda.cu:277-282 — stable sort of (hash, index) pairs by hash. */
 void sortParticles(uint* dGridParticleHash, uint* dGridParticleIndex, uint numParticles);
+/* No counterpart in the reference.  The same stable sort as sortParticles,
+ * for callers that cannot allocate device memory: those whose device memory
+ * is owned in full by another allocator (a framework's caching allocator, a
+ * budget fixed at start-up) and those whose timing-critical loop cannot take
+ * cudaMalloc's implicit device-wide synchronisation.  Its scratch is one
+ * fixed array compiled into the library (about 2.4 MB, held by every GPU that
+ * loads the library until the process exits); it calls no allocator.
+ * At most 262,144 keys: larger counts return NW_ERR_INVALID (2) and leave
+ * the arrays untouched.  Returns an nw_status (0 = OK).  The first call on a
+ * device looks up the array's device address, so make that first call before
+ * any stream capture.  All calls share the one array; calls that overlap on
+ * the GPU race.  Runs on the legacy default stream, like sortParticles. */
+int nw_sort_particles_noalloc(uint* dGridParticleHash, uint* dGridParticleIndex, uint numParticles);
 /* particleSystem_cuda.cu:284-306 — random filament reversal. */
 void reverseFilaments(float* force, float* forceOld, float* vel, float* pos, float* uniform, uint numFilaments);
 /* particleSystem_cuda.cu:308-328 — f += -gamma v + N(0, sqrt(2 gamma kT)). */

@@ -215,6 +215,7 @@ LEGACY_API = [
     ("collideSolvent", None, [_fp, _fp, _fp, _fp, _u32, _u32]),
     ("filamentForces", None, [_fp, _fp, _fp, _f32]),
     ("sortParticles", None, [_fp, _fp, _u32]),
+    ("nw_sort_particles_noalloc", C.c_int, [_fp, _fp, _u32]),
     ("reverseFilaments", None, [_fp, _fp, _fp, _fp, _fp, _u32]),
     ("langevinThermostat", None, [_fp, _fp, _fp, _f32, _f32, _u32]),
     ("solventCellCentorOfMomentum", None, [_fp, _fp, _fp, _fp, _fp, _u32]),
