@@ -67,6 +67,13 @@ def alg_bytes(name: str, cfg) -> float:
         # sorted position + index read, force read-modify-write, cell bounds read
         "pair_wca": 52.0 * nb + 8.0 * C,
         "pair_ref": 84.0 * nb + 8.0 * C,
+        # cell-list path: pro = integrate .. hash + list insert (r, v, f, f_old in; r, v, f_old, f,
+        # tangent, hash, list slot out; list count update and clearing per cell)
+        "bead_pro": 156.0 * nb + 8.0 * C,
+        # epi: own position, force read-modify-write, list counts
+        "bead_epi": 48.0 * nb + 4.0 * C,
+        # fused = epi(n) + pro(n+1) with the complete force kept in a register
+        "bead_fused": 156.0 * nb + 12.0 * C,
         # position read, hash + slot written
         "srd_hash": 24.0 * nt,
         # member index + velocity read/write; solvent position read/write; cell offsets + mean

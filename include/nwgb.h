@@ -140,8 +140,22 @@ typedef struct NwConfig {
     /* run control */
     uint64_t seed;
     float    dt;
-    uint32_t reserved[7];
+    int32_t  strategy;         /* nw_strategy: how a step finds its neighbours */
+    uint32_t cell_capacity;    /* beads a cell list holds (NW_STRATEGY_CELL_LISTS): 8 or 16; 0 = by model */
+    uint32_t reserved[5];
 } NwConfig;
+
+/* Neighbour search of the bead step.
+ *  SORTED      stable counting sort of the beads by cell, cell start/end and
+ *              cell-ordered copies every step (the reference's scheme); five
+ *              kernels per step, no occupancy limit.
+ *  CELL_LISTS  capped per-cell bead lists; the pair pass of one step and the
+ *              integrate/bonded pass of the next run as one kernel; the
+ *              sorted order and cell bounds are produced only when read.
+ *              A cell with more beads than cell_capacity is reported as
+ *              NW_ERR_CELL_OVERFLOW.
+ *  AUTO        CELL_LISTS. */
+typedef enum { NW_STRATEGY_AUTO = 0, NW_STRATEGY_SORTED = 1, NW_STRATEGY_CELL_LISTS = 2 } nw_strategy;
 
 /* Array selectors for nw_get_array / nw_set_array / nw_device_array. */
 typedef enum {

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "nw_engine.h"
+#include "nw_fused.cuh"
 
 namespace nw {
 
@@ -68,14 +69,6 @@ DevParams make_dev_params(const NwConfig& c, float dt)
 
 static uint32_t cdiv(uint64_t a, uint32_t b) { return (uint32_t)((a + b - 1) / b); }
 
-// Filaments per block of the filament pass: whole filaments, about 256 threads.
-static uint32_t filaments_per_block(uint32_t L, uint32_t nf)
-{
-    uint32_t fpb = L >= 256 ? 1u : 256u / L;
-    if (fpb > nf && nf > 0) fpb = nf;
-    return fpb ? fpb : 1u;
-}
-
 void Prof::mark(const char* name)
 {
     cudaEvent_t e;
@@ -108,7 +101,7 @@ uint64_t enqueue_bead_step(const DevParams& P, const StepBuffers& B, uint32_t nc
                            cudaStream_t s, Prof* prof)
 {
     if (P.nb == 0) return 0;
-    const uint32_t fpb = filaments_per_block(P.L, P.nf);
+    const uint32_t fpb = list_filaments_per_block(P.L, P.nf);
     const uint32_t beads = fpb * P.L;
     const uint32_t threads = (beads + 31u) & ~31u;
     const size_t smem = (size_t)beads * sizeof(float4) * (P.reverse_on ? 3u : 1u);
@@ -136,11 +129,11 @@ uint64_t enqueue_bead_step(const DevParams& P, const StepBuffers& B, uint32_t nc
 }
 
 uint64_t enqueue_srd(const DevParams& P, const StepBuffers& B, uint32_t srd_nchunks, uint32_t step_off, float dt_srd,
-                     int shift_from_step, float3 shift, cudaStream_t s, Prof* prof)
+                     int shift_from_step, float3 shift, cudaStream_t s, Prof* prof, uint32_t buf_sel)
 {
     if (P.ntotal == 0) return 0;
     NW_MARK("srd_hash");
-    srd_hash_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(P, B, step_off, shift_from_step, shift);
+    srd_hash_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(P, B, step_off, shift_from_step, shift, buf_sel);
     NW_MARK("srd_chunk_sum");
     chunk_sum_kernel<<<srd_nchunks, 512, 0, s>>>(B.srd_count, P.srd_ncells, B.srd_chunk);
     NW_MARK("srd_scan_cells");
@@ -149,8 +142,17 @@ uint64_t enqueue_srd(const DevParams& P, const StepBuffers& B, uint32_t srd_nchu
     NW_MARK("srd_scatter");
     scatter_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(B.srd_hash, B.srd_slot, B.srd_offset, B.srd_tmp, P.ntotal);
     NW_MARK("srd_collide");
-    srd_collide_kernel<<<cdiv(P.srd_ncells, 256), 256, 0, s>>>(P, B, step_off, dt_srd);
+    srd_collide_kernel<<<cdiv(P.srd_ncells, 256), 256, 0, s>>>(P, B, step_off, dt_srd, buf_sel);
     return 5;
+}
+
+// Histogram of bead hashes (the counting sort's first pass, for the sorted
+// order and cell bounds read from a cell-list system).
+__global__ void __launch_bounds__(256) count_hash_kernel(const uint32_t* __restrict__ hash, uint32_t n,
+                                                         uint32_t* __restrict__ count, uint32_t* __restrict__ slot)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) slot[i] = count_into_cell(count, hash[i]);
 }
 
 }  // namespace nw
@@ -172,10 +174,13 @@ struct nw_system {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     StepBuffers B;
+    bool lists = false;  // NW_STRATEGY_CELL_LISTS
     uint32_t nb = 0, ns = 0, ntotal = 0, ncells = 0, nchunks = 0, srd_ncells = 0, srd_nchunks = 0;
     uint64_t step = 0;
     uint64_t version = 1;
     bool use_graphs = true;
+    bool lists_dirty = false;  // list counters must be cleared before the next update
+    uint64_t sorted_for = ~0ull;  // step whose sorted order / cell bounds are in the sort buffers
     std::vector<GraphEntry> graphs;
     uint64_t last_launches = 0;
     std::vector<void*> allocs;
@@ -218,51 +223,6 @@ void drop_graphs(nw_system* s)
     s->version++;
 }
 
-struct ArrayInfo {
-    void* ptr;
-    size_t elem;
-    size_t count;
-};
-
-ArrayInfo array_info(nw_system* s, int array)
-{
-    const StepBuffers& B = s->B;
-    switch (array) {
-    case NW_POSITION: return {B.pos, sizeof(float4), s->ntotal};
-    case NW_VELOCITY: return {B.vel, sizeof(float4), s->ntotal};
-    case NW_TANGENT: return {B.tangent, sizeof(float4), s->nb};
-    case NW_FORCE: return {B.force, sizeof(float4), s->nb};
-    case NW_FORCE_OLD: return {B.force_old, sizeof(float4), s->nb};
-    case NW_HASH: return {B.hash, sizeof(uint32_t), s->nb};
-    case NW_SORTED_INDEX: return {B.sorted_index, sizeof(uint32_t), s->nb};
-    case NW_CELL_START: return {B.cell_start, sizeof(uint32_t), s->ncells};
-    case NW_CELL_END: return {B.cell_end, sizeof(uint32_t), s->ncells};
-    case NW_SRD_SORTED_INDEX: return {B.srd_sorted_index, sizeof(uint32_t), s->cfg.srd_enabled ? s->ntotal : 0u};
-    case NW_SRD_CELL_START: return {B.srd_start, sizeof(uint32_t), s->cfg.srd_enabled ? s->srd_ncells : 0u};
-    case NW_SRD_CELL_END: return {B.srd_end, sizeof(uint32_t), s->cfg.srd_enabled ? s->srd_ncells : 0u};
-    case NW_SRD_CELL_MEAN: return {B.srd_mean, sizeof(float4), s->cfg.srd_enabled ? s->srd_ncells : 0u};
-    default: return {nullptr, 0, 0};
-    }
-}
-
-// Enqueue `nsteps` steps starting at device step base + 0 and advance the base.
-uint64_t enqueue_steps(nw_system* s, int nsteps, float dt, uint64_t first_step, Prof* prof = nullptr)
-{
-    const DevParams P = make_dev_params(s->cfg, dt);
-    uint64_t launches = 0;
-    for (int j = 0; j < nsteps; ++j) {
-        launches += enqueue_bead_step(P, s->B, s->nchunks, (uint32_t)j, dt, s->stream, prof);
-        const uint64_t st = first_step + (uint64_t)j;
-        if (s->cfg.srd_enabled && (st % s->cfg.srd_gap) == 0)
-            launches += enqueue_srd(P, s->B, s->srd_nchunks, (uint32_t)j, dt * (float)s->cfg.srd_gap, 1,
-                                    make_float3(0.f, 0.f, 0.f), s->stream, prof);
-    }
-    if (prof) prof->mark("advance_step");
-    advance_step_kernel<<<1, 1, 0, s->stream>>>(s->B.step_base, (unsigned long long)nsteps);
-    if (prof) prof->end();
-    return launches + 1;
-}
-
 nw_status cuda_status(cudaError_t e)
 {
     if (e == cudaSuccess) return NW_OK;
@@ -270,6 +230,148 @@ nw_status cuda_status(cudaError_t e)
     if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return NW_ERR_NO_DEVICE;
     std::fprintf(stderr, "[nwgb] CUDA error: %s\n", cudaGetErrorString(e));
     return NW_ERR_CUDA;
+}
+
+// Bead buffer holding the state after the last update.
+uint32_t cur_buffer(const nw_system* s) { return s->lists ? (uint32_t)((s->step + 1ull) & 1ull) : 0u; }
+
+// Clear the list counters when the step counter changed under them.
+cudaError_t clean_lists(nw_system* s)
+{
+    if (!s->lists || !s->lists_dirty) return cudaSuccess;
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+        e = cudaMemsetAsync(s->B.lcount[k], 0, ((size_t)s->ncells + 8) * 4, s->stream);
+    if (e == cudaSuccess) s->lists_dirty = false;
+    return e;
+}
+
+// Enqueue `nsteps` updates starting at device step base + 0 and advance the base.
+uint64_t enqueue_steps(nw_system* s, int nsteps, float dt, uint64_t first_step, Prof* prof = nullptr)
+{
+    const DevParams P = make_dev_params(s->cfg, dt);
+    const bool srd = s->cfg.srd_enabled != 0;
+    const uint32_t gap = s->cfg.srd_gap ? s->cfg.srd_gap : 1u;
+    const float dt_srd = dt * (float)gap;
+    uint64_t launches = 0;
+    if (!s->lists) {
+        for (int j = 0; j < nsteps; ++j) {
+            launches += enqueue_bead_step(P, s->B, s->nchunks, (uint32_t)j, dt, s->stream, prof);
+            if (srd && ((first_step + (uint64_t)j) % gap) == 0)
+                launches += enqueue_srd(P, s->B, s->srd_nchunks, (uint32_t)j, dt_srd, 1, make_float3(0.f, 0.f, 0.f),
+                                        s->stream, prof, 2u);
+        }
+    } else {
+        NW_MARK("bead_pro");
+        launches += launch_bead_pro(P, s->B, 0u, dt, s->stream);
+        for (int j = 0; j < nsteps; ++j) {
+            const bool srd_now = srd && ((first_step + (uint64_t)j) % gap) == 0;
+            if (j == nsteps - 1 || srd_now) {
+                NW_MARK("bead_epi");
+                launches += launch_bead_epi(P, s->B, (uint32_t)j, s->stream);
+                if (srd_now)
+                    launches += enqueue_srd(P, s->B, s->srd_nchunks, (uint32_t)j, dt_srd, 1,
+                                            make_float3(0.f, 0.f, 0.f), s->stream, prof, 2u);
+                if (j < nsteps - 1) {
+                    NW_MARK("bead_pro");
+                    launches += launch_bead_pro(P, s->B, (uint32_t)(j + 1), dt, s->stream);
+                }
+            } else {
+                NW_MARK("bead_fused");
+                launches += launch_bead_fused(P, s->B, (uint32_t)j, dt, s->stream);
+            }
+        }
+    }
+    if (prof) prof->mark("advance_step");
+    advance_step_kernel<<<1, 1, 0, s->stream>>>(s->B.step_base, (unsigned long long)nsteps);
+    if (prof) prof->end();
+    return launches + 1;
+}
+
+// Sorted order and cell bounds of the current bead hashes (cell-list systems
+// keep no sorted order between updates; this runs the counting sort once).
+cudaError_t ensure_sorted(nw_system* s)
+{
+    if (!s->lists || s->sorted_for == s->step || s->nb == 0) return cudaSuccess;
+    const DevParams P = make_dev_params(s->cfg, s->cfg.dt);
+    StepBuffers B = s->B;
+    const uint32_t cur = cur_buffer(s);
+    B.hash = B.hash2[cur];
+    B.pos = B.pos2[cur];
+    count_hash_kernel<<<cdiv(s->nb, 256), 256, 0, s->stream>>>(B.hash, s->nb, B.cell_count, B.slot);
+    chunk_sum_kernel<<<s->nchunks, 512, 0, s->stream>>>(B.cell_count, P.ncells, B.chunk_count);
+    scan_cells_kernel<true><<<s->nchunks, 512, 0, s->stream>>>(B.cell_count, B.chunk_count, P.ncells, B.cell_offset,
+                                                               B.cell_start, B.cell_end);
+    scatter_kernel<<<cdiv(s->nb, 256), 256, 0, s->stream>>>(B.hash, B.slot, B.cell_offset, B.tmp_index, s->nb);
+    stable_gather_kernel<false><<<cdiv(s->nb, 256), 256, 0, s->stream>>>(P, B);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) s->sorted_for = s->step;
+    return e;
+}
+
+enum class Dir { ToDevice, ToHost };
+
+// Copy `count` elements of an API array between host and device.  Position /
+// velocity arrays are beads [0, nb) then solvent [nb, nb + ns) in two stores.
+nw_status transfer(nw_system* s, int array, void* host, uint32_t start, uint32_t count, Dir dir)
+{
+    const uint32_t cur = cur_buffer(s);
+    const StepBuffers& B = s->B;
+    void* bead_ptr = nullptr;
+    void* solv_ptr = nullptr;
+    size_t elem = 16;
+    size_t nbead = s->nb, ntot = s->nb;
+    switch (array) {
+    case NW_POSITION: bead_ptr = B.pos2[cur]; solv_ptr = B.spos; ntot = s->ntotal; break;
+    case NW_VELOCITY: bead_ptr = B.vel2[cur]; solv_ptr = B.svel; ntot = s->ntotal; break;
+    case NW_TANGENT: bead_ptr = B.tan2[cur]; break;
+    case NW_FORCE: bead_ptr = B.force; break;
+    case NW_FORCE_OLD: bead_ptr = B.force_old; break;
+    case NW_HASH: bead_ptr = B.hash2[cur]; elem = 4; break;
+    case NW_SORTED_INDEX:
+    case NW_CELL_START:
+    case NW_CELL_END: {
+        if (dir == Dir::ToDevice) return NW_ERR_INVALID;
+        cudaError_t e = ensure_sorted(s);
+        if (e != cudaSuccess) return cuda_status(e);
+        elem = 4;
+        if (array == NW_SORTED_INDEX) bead_ptr = B.sorted_index;
+        else {
+            bead_ptr = array == NW_CELL_START ? B.cell_start : B.cell_end;
+            nbead = ntot = s->ncells;
+        }
+        break;
+    }
+    case NW_SRD_SORTED_INDEX: bead_ptr = B.srd_sorted_index; elem = 4; nbead = ntot = s->cfg.srd_enabled ? s->ntotal : 0; break;
+    case NW_SRD_CELL_START: bead_ptr = B.srd_start; elem = 4; nbead = ntot = s->cfg.srd_enabled ? s->srd_ncells : 0; break;
+    case NW_SRD_CELL_END: bead_ptr = B.srd_end; elem = 4; nbead = ntot = s->cfg.srd_enabled ? s->srd_ncells : 0; break;
+    case NW_SRD_CELL_MEAN: bead_ptr = B.srd_mean; nbead = ntot = s->cfg.srd_enabled ? s->srd_ncells : 0; break;
+    default: return NW_ERR_INVALID;
+    }
+    if ((uint64_t)start + count > ntot) return NW_ERR_INVALID;
+    if (!count) return NW_OK;
+    if (dir == Dir::ToDevice && (array == NW_HASH || array >= NW_SRD_SORTED_INDEX)) return NW_ERR_INVALID;
+    cudaError_t e = cudaSuccess;
+    char* h = static_cast<char*>(host);
+    const uint64_t end = (uint64_t)start + count;
+    // bead part
+    if (start < nbead) {
+        const uint64_t a = start, b = end < nbead ? end : nbead;
+        char* d = static_cast<char*>(bead_ptr) + a * elem;
+        e = dir == Dir::ToDevice ? cudaMemcpyAsync(d, h, (b - a) * elem, cudaMemcpyHostToDevice, s->stream)
+                                 : cudaMemcpyAsync(h, d, (b - a) * elem, cudaMemcpyDeviceToHost, s->stream);
+        h += (b - a) * elem;
+    }
+    // solvent part
+    if (e == cudaSuccess && end > nbead) {
+        const uint64_t a = start > nbead ? start : nbead, b = end;
+        char* d = static_cast<char*>(solv_ptr) + (a - nbead) * elem;
+        e = dir == Dir::ToDevice ? cudaMemcpyAsync(d, h, (b - a) * elem, cudaMemcpyHostToDevice, s->stream)
+                                 : cudaMemcpyAsync(h, d, (b - a) * elem, cudaMemcpyDeviceToHost, s->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (dir == Dir::ToDevice) s->sorted_for = ~0ull;
+    return cuda_status(e);
 }
 
 }  // namespace
@@ -295,6 +397,7 @@ nw_status nw_create(const NwConfig* cfg, nw_system** out)
         return NW_ERR_CUDA;
     }
     s->stream = s->own_stream;
+    s->lists = cfg->strategy != NW_STRATEGY_SORTED;
     s->nb = cfg->num_filaments * cfg->filament_size;
     s->ns = cfg->srd_enabled ? cfg->num_solvent : 0u;
     s->ntotal = s->nb + s->ns;
@@ -304,18 +407,34 @@ nw_status nw_create(const NwConfig* cfg, nw_system** out)
     s->srd_nchunks = (s->srd_ncells + kChunk - 1) / kChunk;
     StepBuffers& B = s->B;
     std::memset(&B, 0, sizeof(B));
-    const size_t nb = s->nb, nt = s->ntotal, C = s->ncells;
+    const size_t nb = s->nb, ns = s->ns, C = s->ncells;
     const bool ref = cfg->model == NW_MODEL_REF_DEM;
+    B.cap = cfg->cell_capacity ? cfg->cell_capacity : (ref ? 16u : 8u);
     st = NW_OK;
     auto A = [&](nw_status x) {
         if (st == NW_OK) st = x;
     };
-    A(alloc_n(s, &B.pos, nt));
-    A(alloc_n(s, &B.vel, nt));
+    const int nbuf = s->lists ? 2 : 1;
+    for (int k = 0; k < nbuf; ++k) {
+        A(alloc_n(s, &B.pos2[k], nb));
+        A(alloc_n(s, &B.vel2[k], nb));
+        A(alloc_n(s, &B.tan2[k], nb));
+        A(alloc_n(s, &B.hash2[k], nb));
+    }
+    if (!s->lists) {
+        B.pos2[1] = B.pos2[0];
+        B.vel2[1] = B.vel2[0];
+        B.tan2[1] = B.tan2[0];
+        B.hash2[1] = B.hash2[0];
+    }
+    B.pos = B.pos2[0];
+    B.vel = B.vel2[0];
+    B.tangent = B.tan2[0];
+    B.hash = B.hash2[0];
     A(alloc_n(s, &B.force, nb));
     A(alloc_n(s, &B.force_old, nb));
-    A(alloc_n(s, &B.tangent, nb));
-    A(alloc_n(s, &B.hash, nb));
+    A(alloc_n(s, &B.spos, ns));
+    A(alloc_n(s, &B.svel, ns));
     A(alloc_n(s, &B.slot, nb));
     A(alloc_n(s, &B.tmp_index, nb));
     A(alloc_n(s, &B.sorted_index, nb));
@@ -326,12 +445,16 @@ nw_status nw_create(const NwConfig* cfg, nw_system** out)
     A(alloc_n(s, &B.cell_end, C + 8));
     A(alloc_n(s, &B.chunk_count, (size_t)s->nchunks + 1));
     A(alloc_n(s, &B.sorted_pos, nb));
-    if (ref) {
+    if (ref && !s->lists) {
         A(alloc_n(s, &B.sorted_vel, nb));
         A(alloc_n(s, &B.sorted_tan, nb));
     }
+    if (s->lists) {
+        for (int k = 0; k < 3; ++k) A(alloc_n(s, &B.lcount[k], C + 8));
+        for (int k = 0; k < 2; ++k) A(alloc_n(s, &B.lslot[k], C * B.cap + 8));
+    }
     if (cfg->srd_enabled) {
-        const size_t Cs = s->srd_ncells;
+        const size_t Cs = s->srd_ncells, nt = s->ntotal;
         A(alloc_n(s, &B.srd_hash, nt));
         A(alloc_n(s, &B.srd_slot, nt));
         A(alloc_n(s, &B.srd_tmp, nt));
@@ -352,16 +475,25 @@ nw_status nw_create(const NwConfig* cfg, nw_system** out)
     }
     // counters must start at zero; state starts empty
     cudaError_t e = cudaSuccess;
-    auto Z = [&](void* p, size_t bytes) {
-        if (p && e == cudaSuccess) e = cudaMemsetAsync(p, 0, bytes, s->stream);
+    auto Z = [&](void* p, size_t bytes, int v = 0) {
+        if (p && e == cudaSuccess) e = cudaMemsetAsync(p, v, bytes, s->stream);
     };
-    Z(B.pos, nt * 16);
-    Z(B.vel, nt * 16);
+    for (int k = 0; k < nbuf; ++k) {
+        Z(B.pos2[k], nb * 16);
+        Z(B.vel2[k], nb * 16);
+        Z(B.tan2[k], nb * 16);
+        Z(B.hash2[k], nb * 4);
+    }
     Z(B.force, nb * 16);
     Z(B.force_old, nb * 16);
-    Z(B.tangent, nb * 16);
+    Z(B.spos, ns * 16);
+    Z(B.svel, ns * 16);
     Z(B.cell_count, (C + 8) * 4);
     Z(B.chunk_count, ((size_t)s->nchunks + 1) * 4);
+    Z(B.cell_start, (C + 8) * 4, 0xff);
+    Z(B.cell_end, (C + 8) * 4, 0xff);
+    if (s->lists)
+        for (int k = 0; k < 3; ++k) Z(B.lcount[k], (C + 8) * 4);
     if (cfg->srd_enabled) {
         Z(B.srd_count, ((size_t)s->srd_ncells + 8) * 4);
         Z(B.srd_chunk, ((size_t)s->srd_nchunks + 1) * 4);
@@ -369,8 +501,6 @@ nw_status nw_create(const NwConfig* cfg, nw_system** out)
     }
     Z(B.err, 16);
     Z(B.step_base, 8);
-    if (e == cudaSuccess) e = cudaMemsetAsync(B.cell_start, 0xff, (C + 8) * 4, s->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(B.cell_end, 0xff, (C + 8) * 4, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     if (e != cudaSuccess) {
         st = cuda_status(e);
@@ -398,7 +528,8 @@ nw_status nw_set_config(nw_system* s, const NwConfig* cfg)
     if (st != NW_OK) return st;
     const NwConfig& o = s->cfg;
     if (cfg->model != o.model || cfg->num_filaments != o.num_filaments || cfg->filament_size != o.filament_size ||
-        cfg->srd_enabled != o.srd_enabled || (cfg->srd_enabled && cfg->num_solvent != o.num_solvent))
+        cfg->srd_enabled != o.srd_enabled || (cfg->srd_enabled && cfg->num_solvent != o.num_solvent) ||
+        cfg->strategy != o.strategy || cfg->cell_capacity != o.cell_capacity)
         return NW_ERR_INVALID;
     for (int a = 0; a < 3; ++a)
         if (cfg->grid[a] != o.grid[a] || (cfg->srd_enabled && cfg->srd_grid[a] != o.srd_grid[a]))
@@ -428,33 +559,46 @@ nw_status nw_get_counts(const nw_system* s, uint32_t* nb, uint32_t* ns, uint32_t
 nw_status nw_set_array(nw_system* s, int array, const void* host, uint32_t start, uint32_t count)
 {
     if (!s || (!host && count)) return NW_ERR_INVALID;
-    ArrayInfo a = array_info(s, array);
-    if (!a.ptr || (uint64_t)start + count > a.count) return NW_ERR_INVALID;
-    if (!count) return NW_OK;
-    cudaError_t e = cudaMemcpyAsync((char*)a.ptr + (size_t)start * a.elem, host, (size_t)count * a.elem,
-                                    cudaMemcpyHostToDevice, s->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    return cuda_status(e);
+    return transfer(s, array, const_cast<void*>(host), start, count, Dir::ToDevice);
 }
 
 nw_status nw_get_array(nw_system* s, int array, void* host, uint32_t start, uint32_t count)
 {
     if (!s || (!host && count)) return NW_ERR_INVALID;
-    ArrayInfo a = array_info(s, array);
-    if (!a.ptr || (uint64_t)start + count > a.count) return NW_ERR_INVALID;
-    if (!count) return NW_OK;
-    cudaError_t e = cudaMemcpyAsync(host, (const char*)a.ptr + (size_t)start * a.elem, (size_t)count * a.elem,
-                                    cudaMemcpyDeviceToHost, s->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    return cuda_status(e);
+    return transfer(s, array, host, start, count, Dir::ToHost);
 }
 
 nw_status nw_device_array(nw_system* s, int array, void** dptr)
 {
     if (!s || !dptr) return NW_ERR_INVALID;
-    ArrayInfo a = array_info(s, array);
-    if (!a.ptr) return NW_ERR_INVALID;
-    *dptr = a.ptr;
+    const uint32_t cur = cur_buffer(s);
+    const StepBuffers& B = s->B;
+    void* p = nullptr;
+    switch (array) {
+    case NW_POSITION: p = B.pos2[cur]; break;
+    case NW_VELOCITY: p = B.vel2[cur]; break;
+    case NW_TANGENT: p = B.tan2[cur]; break;
+    case NW_FORCE: p = B.force; break;
+    case NW_FORCE_OLD: p = B.force_old; break;
+    case NW_HASH: p = B.hash2[cur]; break;
+    case NW_SORTED_INDEX:
+    case NW_CELL_START:
+    case NW_CELL_END: {
+        cudaError_t e = ensure_sorted(s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) return cuda_status(e);
+        p = array == NW_SORTED_INDEX ? (void*)B.sorted_index : array == NW_CELL_START ? (void*)B.cell_start
+                                                                                      : (void*)B.cell_end;
+        break;
+    }
+    case NW_SRD_SORTED_INDEX: p = B.srd_sorted_index; break;
+    case NW_SRD_CELL_START: p = B.srd_start; break;
+    case NW_SRD_CELL_END: p = B.srd_end; break;
+    case NW_SRD_CELL_MEAN: p = B.srd_mean; break;
+    default: return NW_ERR_INVALID;
+    }
+    if (!p) return NW_ERR_INVALID;
+    *dptr = p;
     return NW_OK;
 }
 
@@ -473,8 +617,9 @@ nw_status nw_step(nw_system* s, int nsteps, float dt)
     if (nsteps == 0) return NW_OK;
     if (!(dt > 0.0f)) dt = s->cfg.dt;
     if (!std::isfinite(dt)) return NW_ERR_INVALID;
+    cudaError_t e = clean_lists(s);
+    if (e != cudaSuccess) return cuda_status(e);
     const uint32_t phase = s->cfg.srd_enabled ? (uint32_t)(s->step % s->cfg.srd_gap) : 0u;
-    cudaError_t e = cudaSuccess;
     if (s->use_graphs && nsteps > 1) {
         uint32_t bits;
         std::memcpy(&bits, &dt, 4);
@@ -541,10 +686,27 @@ nw_status nw_get_step(const nw_system* s, uint64_t* step)
 nw_status nw_set_step(nw_system* s, uint64_t step)
 {
     if (!s) return NW_ERR_INVALID;
+    if (s->lists && ((step ^ s->step) & 1ull)) {
+        // keep the state in the buffer the new step count names as current
+        const uint32_t from = cur_buffer(s), to = from ^ 1u;
+        const size_t nb = s->nb;
+        cudaError_t e = cudaMemcpyAsync(s->B.pos2[to], s->B.pos2[from], nb * 16, cudaMemcpyDeviceToDevice, s->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s->B.vel2[to], s->B.vel2[from], nb * 16, cudaMemcpyDeviceToDevice, s->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s->B.tan2[to], s->B.tan2[from], nb * 16, cudaMemcpyDeviceToDevice, s->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s->B.hash2[to], s->B.hash2[from], nb * 4, cudaMemcpyDeviceToDevice, s->stream);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
     unsigned long long v = step;
     cudaError_t e = cudaMemcpyAsync(s->B.step_base, &v, 8, cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    if (e == cudaSuccess) s->step = step;
+    if (e == cudaSuccess) {
+        s->step = step;
+        s->lists_dirty = true;
+        s->sorted_for = ~0ull;
+    }
     return cuda_status(e);
 }
 
@@ -570,7 +732,7 @@ nw_status nw_srd_collide(nw_system* s, float dt_srd, const float shift[3])
     if (!s->cfg.srd_enabled) return NW_ERR_UNSUPPORTED;
     const DevParams P = make_dev_params(s->cfg, s->cfg.dt);
     s->last_launches = enqueue_srd(P, s->B, s->srd_nchunks, 0u, dt_srd, 0, make_float3(shift[0], shift[1], shift[2]),
-                                   s->stream);
+                                   s->stream, nullptr, cur_buffer(s));
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     return cuda_status(e);
@@ -599,7 +761,7 @@ nw_status nw_checkpoint_save(nw_system* s, void* buf, size_t bytes)
     CkptHeader h;
     std::memset(&h, 0, sizeof(h));
     std::memcpy(h.magic, "NWGBCKP", 8);
-    h.version = 1;
+    h.version = 2;
     h.cfg_bytes = sizeof(NwConfig);
     h.nb = s->nb;
     h.ntotal = s->ntotal;
@@ -608,18 +770,14 @@ nw_status nw_checkpoint_save(nw_system* s, void* buf, size_t bytes)
     p += sizeof(h);
     std::memcpy(p, &s->cfg, sizeof(NwConfig));
     p += sizeof(NwConfig);
-    struct {
-        void* d;
-        size_t n;
-    } parts[] = {{s->B.pos, (size_t)s->ntotal * 16}, {s->B.vel, (size_t)s->ntotal * 16}, {s->B.force, (size_t)s->nb * 16},
-                 {s->B.force_old, (size_t)s->nb * 16}, {s->B.tangent, (size_t)s->nb * 16}};
-    cudaError_t e = cudaSuccess;
-    for (auto& q : parts) {
-        if (q.n && e == cudaSuccess) e = cudaMemcpyAsync(p, q.d, q.n, cudaMemcpyDeviceToHost, s->stream);
-        p += q.n;
+    const int arrays[] = {NW_POSITION, NW_VELOCITY, NW_FORCE, NW_FORCE_OLD, NW_TANGENT};
+    for (int a : arrays) {
+        const uint32_t n = (a == NW_POSITION || a == NW_VELOCITY) ? s->ntotal : s->nb;
+        nw_status st = transfer(s, a, p, 0, n, Dir::ToHost);
+        if (st != NW_OK) return st;
+        p += (size_t)n * 16;
     }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    return cuda_status(e);
+    return NW_OK;
 }
 
 nw_status nw_checkpoint_load(nw_system* s, const void* buf, size_t bytes)
@@ -629,7 +787,7 @@ nw_status nw_checkpoint_load(nw_system* s, const void* buf, size_t bytes)
     const char* p = (const char*)buf;
     CkptHeader h;
     std::memcpy(&h, p, sizeof(h));
-    if (std::memcmp(h.magic, "NWGBCKP", 8) != 0 || h.version != 1 || h.cfg_bytes != sizeof(NwConfig) ||
+    if (std::memcmp(h.magic, "NWGBCKP", 8) != 0 || h.version != 2 || h.cfg_bytes != sizeof(NwConfig) ||
         h.nb != s->nb || h.ntotal != s->ntotal)
         return NW_ERR_INVALID;
     p += sizeof(h);
@@ -638,19 +796,16 @@ nw_status nw_checkpoint_load(nw_system* s, const void* buf, size_t bytes)
     p += sizeof(NwConfig);
     nw_status st = nw_set_config(s, &cfg);
     if (st != NW_OK) return st;
-    struct {
-        void* d;
-        size_t n;
-    } parts[] = {{s->B.pos, (size_t)s->ntotal * 16}, {s->B.vel, (size_t)s->ntotal * 16}, {s->B.force, (size_t)s->nb * 16},
-                 {s->B.force_old, (size_t)s->nb * 16}, {s->B.tangent, (size_t)s->nb * 16}};
-    cudaError_t e = cudaSuccess;
-    for (auto& q : parts) {
-        if (q.n && e == cudaSuccess) e = cudaMemcpyAsync(q.d, p, q.n, cudaMemcpyHostToDevice, s->stream);
-        p += q.n;
+    st = nw_set_step(s, h.step);
+    if (st != NW_OK) return st;
+    const int arrays[] = {NW_POSITION, NW_VELOCITY, NW_FORCE, NW_FORCE_OLD, NW_TANGENT};
+    for (int a : arrays) {
+        const uint32_t n = (a == NW_POSITION || a == NW_VELOCITY) ? s->ntotal : s->nb;
+        st = transfer(s, a, const_cast<char*>(p), 0, n, Dir::ToDevice);
+        if (st != NW_OK) return st;
+        p += (size_t)n * 16;
     }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    if (e != cudaSuccess) return cuda_status(e);
-    return nw_set_step(s, h.step);
+    return NW_OK;
 }
 
 nw_status nw_last_launch_count(const nw_system* s, uint64_t* launches)
@@ -664,10 +819,12 @@ nw_status nw_profile_steps(nw_system* s, int nsteps, float dt, NwKernelTime* out
 {
     if (!s || nsteps < 1 || !out || max_entries < 1 || !n_entries) return NW_ERR_INVALID;
     if (!(dt > 0.0f)) dt = s->cfg.dt;
+    cudaError_t e = clean_lists(s);
+    if (e != cudaSuccess) return cuda_status(e);
     Prof prof;
     prof.stream = s->stream;
     s->last_launches = enqueue_steps(s, nsteps, dt, s->step, &prof);
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     if (e != cudaSuccess) {
         prof.clear();

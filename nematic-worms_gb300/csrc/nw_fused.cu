@@ -1,0 +1,468 @@
+// nw_fused.cu — the cell-list step path: capped per-cell bead lists instead
+// of a full sort, and the pair pass of update n fused with the integrate /
+// bonded / hash pass of update n + 1 in one kernel.
+//
+// Update n (ParticleSystem::update, simulation/particleSystem.cpp:249-339) is
+//   pro(n): integrate -> [reverse] -> Langevin -> bending, tangents [bonds,
+//           drive] -> cell hash -> insert into list n      (reads buffers n-1)
+//   epi(n): pair forces from list n, force[i] = F_n complete (reads buffers n)
+// and a call of M updates launches pro(s), then fused(n -> n+1) = epi(n) +
+// pro(n+1) for every n not followed by an SRD collision, and epi(last).
+// Bead state is double-buffered ([n & 1] written by update n), so a block
+// integrating update n+1 never overwrites positions another block still reads
+// for the pair forces of update n.  Members of a cell are visited in
+// ascending bead index (a sorting network over the cell's slots), which is
+// the order of the reference's stable sort: forces accumulate in the same
+// order as with the sorted arrays, and runs are bit-identical.
+#include "nw_fused.cuh"
+
+namespace nw {
+namespace {
+
+// Ascending bitonic sort of N (power of two) registers, fully unrolled.
+template <int N>
+__device__ __forceinline__ void bitonic_sort(uint32_t (&a)[N])
+{
+#pragma unroll
+    for (int size = 2; size <= N; size <<= 1)
+#pragma unroll
+        for (int stride = size / 2; stride > 0; stride >>= 1)
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+                const int j = i ^ stride;
+                if (j > i) {
+                    const bool up = (i & size) == 0;
+                    const uint32_t x = a[i], y = a[j];
+                    if ((x > y) == up) {
+                        a[i] = y;
+                        a[j] = x;
+                    }
+                }
+            }
+}
+
+// Members of cell c in ascending index; returns their number (<= CAP).
+template <int CAP>
+__device__ __forceinline__ int cell_members(const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ slots,
+                                            uint32_t c, uint32_t (&ids)[CAP])
+{
+    uint32_t k = __ldg(cnt + c);
+    if (k == 0) return 0;
+    if (k > (uint32_t)CAP) k = CAP;  // the overflow was flagged when the list was filled
+    const uint4* src = reinterpret_cast<const uint4*>(slots + (size_t)c * CAP);
+#pragma unroll
+    for (int q = 0; q < CAP / 4; ++q) {
+        uint4 v = make_uint4(kEmpty, kEmpty, kEmpty, kEmpty);
+        if ((uint32_t)(4 * q) < k) v = __ldg(src + q);
+        ids[4 * q] = v.x;
+        ids[4 * q + 1] = v.y;
+        ids[4 * q + 2] = v.z;
+        ids[4 * q + 3] = v.w;
+    }
+#pragma unroll
+    for (int m = 0; m < CAP; ++m)
+        if ((uint32_t)m >= k) ids[m] = kEmpty;
+    if (k == 2) {
+        if (ids[0] > ids[1]) {
+            const uint32_t t = ids[0];
+            ids[0] = ids[1];
+            ids[1] = t;
+        }
+    } else if (k > 2) {
+        bitonic_sort<CAP>(ids);
+    }
+    return (int)k;
+}
+
+// WCA_WORMS pair force on bead i from the lists (distinct neighbour cells in
+// z, y, x order; same law, exclusion and order as pair_wca_kernel).
+template <int CAP>
+__device__ __forceinline__ float3 wca_list_force(const DevParams& P, const float4* __restrict__ pos,
+                                                 const uint32_t* __restrict__ cnt,
+                                                 const uint32_t* __restrict__ slots, uint32_t i, float3 r)
+{
+    const int3 g = grid_pos(P, r);
+    uint32_t cx[3], cy[3], cz[3];
+    const int nx = axis_cells(P, 0, cell_coord(P, 0, g.x), cx);
+    const int ny = axis_cells(P, 1, cell_coord(P, 1, g.y), cy);
+    const int nz = axis_cells(P, 2, cell_coord(P, 2, g.z), cz);
+    const uint32_t fI = i / P.L;
+    float3 f = zero3();
+    for (int kz = 0; kz < nz; ++kz)
+        for (int ky = 0; ky < ny; ++ky)
+            for (int kx = 0; kx < nx; ++kx) {
+                const uint32_t h = (cz[kz] * P.grid[1] + cy[ky]) * P.grid[0] + cx[kx];
+                uint32_t ids[CAP];
+                const int k = cell_members<CAP>(cnt, slots, h, ids);
+#pragma unroll
+                for (int m = 0; m < CAP; ++m) {
+                    if (m >= k) break;
+                    const uint32_t j = ids[m];
+                    if (j == i) continue;
+                    const int d = (int)j - (int)i;
+                    if (d <= P.lj_exclude && d >= -P.lj_exclude && j / P.L == fI) continue;
+                    float3 dr = f3(__ldg(pos + j)) - r;
+                    min_image(P, dr);
+                    const float rr = dot3(dr, dr);
+                    if (rr > P.lj_rc2) continue;
+                    const float rr4 = rr * rr * rr * rr;
+                    const float rr7 = rr * rr * rr * rr * rr * rr * rr;
+                    const float fm = P.lj_amp * ((P.lj_two_s6 / rr7) - (1.0f / rr4));
+                    f.x -= fm * dr.x;
+                    f.y -= fm * dr.y;
+                    f.z -= fm * dr.z;
+                }
+            }
+    return f;
+}
+
+// collideCell over one list cell (particles_kernel_impl.cuh:492-556).
+template <int CAP>
+__device__ __forceinline__ float3 ref_list_cell(const DevParams& P, const float4* __restrict__ pos,
+                                                const float4* __restrict__ vel, const float4* __restrict__ tan,
+                                                const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ slots,
+                                                uint32_t h, uint32_t i, float3 r, float3 v, float3 t, uint32_t fI,
+                                                uint32_t cI)
+{
+    float3 sum = zero3();
+    uint32_t ids[CAP];
+    const int k = cell_members<CAP>(cnt, slots, h, ids);
+    const float cd = P.radius + P.radius;
+#pragma unroll
+    for (int m = 0; m < CAP; ++m) {
+        if (m >= k) break;
+        const uint32_t j = ids[m];
+        if (j == i) continue;
+        const float3 r2 = f3(__ldg(pos + j));
+        const uint32_t fJ = j / P.L, cJ = j - fJ * P.L;
+        const bool same = fI == fJ;
+        if (same && ((cI + 1u == cJ) || (cI - 1u == cJ))) {
+            float3 rel = r2 - r;
+            const float d = min_image_len(P, rel);
+            const float3 nrm = rel / d;
+            sum += (-P.bond_k * (P.bond_r0 - d)) * nrm;
+        } else {
+            float3 rel = r2 - r;
+            const float d = min_image_len(P, rel);
+            if (d < cd) {
+                const float3 nrm = rel / d;
+                const float3 rv = f3(__ldg(vel + j)) - v;
+                const float3 tv = rv - dot3(rv, nrm) * nrm;
+                float3 F = (-P.spring * (cd - d)) * nrm;
+                F += P.damping * rv;
+                F += P.shear * tv;
+                sum += F;
+            }
+        }
+        if (!same) {
+            float3 rel = r2 - r;
+            const float d = min_image_len(P, rel);
+            const float3 t2 = f3(__ldg(tan + j));
+            if (dot3(t, t2) < -0.5f) sum += ((-P.activity) * (t - t2)) / (2.0f * d);
+        }
+    }
+    return sum;
+}
+
+// REF_DEM pair force on bead i: the reference's 27 offsets in z, y, x order;
+// with one z layer each (x, y) cell sum is reused for the three z offsets.
+template <int CAP>
+__device__ __forceinline__ float3 ref_list_force(const DevParams& P, const float4* __restrict__ pos,
+                                                 const float4* __restrict__ vel, const float4* __restrict__ tan,
+                                                 const uint32_t* __restrict__ cnt,
+                                                 const uint32_t* __restrict__ slots, uint32_t i, float3 r)
+{
+    const float3 v = f3(__ldg(vel + i));
+    const float3 t = f3(__ldg(tan + i));
+    const int3 g = grid_pos(P, r);
+    const uint32_t fI = i / P.L, cI = i - fI * P.L;
+    float3 total = zero3();
+    if (P.grid[2] == 1u) {
+        float3 cs[9];
+#pragma unroll
+        for (int y = -1; y <= 1; ++y)
+#pragma unroll
+            for (int x = -1; x <= 1; ++x) {
+                const uint32_t h =
+                    cell_hash(P, cell_coord(P, 0, g.x + x), cell_coord(P, 1, g.y + y), cell_coord(P, 2, g.z));
+                cs[(y + 1) * 3 + (x + 1)] = ref_list_cell<CAP>(P, pos, vel, tan, cnt, slots, h, i, r, v, t, fI, cI);
+            }
+#pragma unroll
+        for (int z = 0; z < 3; ++z)
+#pragma unroll
+            for (int k = 0; k < 9; ++k) total += cs[k];
+    } else {
+        for (int z = -1; z <= 1; ++z)
+            for (int y = -1; y <= 1; ++y)
+                for (int x = -1; x <= 1; ++x) {
+                    const uint32_t h =
+                        cell_hash(P, cell_coord(P, 0, g.x + x), cell_coord(P, 1, g.y + y), cell_coord(P, 2, g.z + z));
+                    total += ref_list_cell<CAP>(P, pos, vel, tan, cnt, slots, h, i, r, v, t, fI, cI);
+                }
+    }
+    return total;
+}
+
+// Pair force of bead i for update n (reads the update-n buffers and list).
+template <int CAP, bool kRef>
+__device__ __forceinline__ float3 list_pair_force(const DevParams& P, const StepBuffers& S, unsigned long long n,
+                                                  uint32_t i)
+{
+    const uint32_t cur = (uint32_t)(n & 1ull);
+    const uint32_t* cnt = S.lcount[(uint32_t)(n % 3ull)];
+    const uint32_t* slots = S.lslot[cur];
+    const float3 r = f3(S.pos2[cur][i]);
+    if (kRef) return ref_list_force<CAP>(P, S.pos2[cur], S.vel2[cur], S.tan2[cur], cnt, slots, i, r);
+    return wca_list_force<CAP>(P, S.pos2[cur], cnt, slots, i, r);
+}
+
+// Shared-memory bytes of the pro part for a block of `beads` beads.
+__host__ __device__ __forceinline__ size_t pro_smem(uint32_t beads, bool reverse)
+{
+    return (size_t)beads * sizeof(float4) * (reverse ? 3u : 1u) + (size_t)beads * 3u * sizeof(float4);
+}
+
+// pro(n) for the block's filaments: every thread of the block must call it.
+// fprev = F_{n-1} of this thread's bead (complete force of the previous update).
+template <int CAP>
+__device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& S, unsigned long long n, float dt,
+                                         uint32_t fpb, bool active, uint32_t i, float3 fprev)
+{
+    extern __shared__ float4 sm[];
+    const uint32_t L = P.L;
+    const uint32_t beads = fpb * L;
+    const uint32_t t = threadIdx.x;
+    const uint32_t w0 = blockIdx.x * fpb;
+    const uint32_t in = (uint32_t)((n + 1ull) & 1ull), out = (uint32_t)(n & 1ull);
+    float4* smp = sm;                                       // positions [beads]
+    float4* smx = sm + (P.reverse_on ? 3u : 1u) * beads;    // triple forces [3][beads]
+
+    // lists of update n+1 must start empty: clear them while nobody reads them
+    {
+        uint32_t* nxt = S.lcount[(uint32_t)((n + 1ull) % 3ull)];
+        const uint32_t stride = gridDim.x * blockDim.x;
+        for (uint32_t c = blockIdx.x * blockDim.x + t; c < P.ncells; c += stride) nxt[c] = 0u;
+    }
+
+    float4 nP = make_float4(0.f, 0.f, 0.f, 0.f), nV = nP, nFo = nP;
+    if (active) {
+        const float4 P4 = S.pos2[in][i], V4 = S.vel2[in][i], Fo4 = S.force_old[i];
+        float3 p = f3(P4), v = f3(V4);
+        const float3 f = fprev, fo = f3(Fo4);
+        // velocity Verlet (particles_kernel_impl.cuh:93-97)
+        const float3 dv = (0.5f * (f + fo)) * dt;
+        v += dv;
+        const float3 dr = v * dt + ((0.5f * f) * dt) * dt;
+        p += dr;
+        apply_boundaries(P, p, v, dr, P.radius);
+        nP = make_float4(p.x, p.y, p.z, P4.w);
+        nV = make_float4(v.x, v.y, v.z, V4.w);
+        nFo = make_float4(f.x, f.y, f.z, Fo4.w);
+    }
+    if (P.reverse_on) {
+        // reverseFilamentsKernel (particles_kernel_impl.cuh:820-857)
+        if (active) {
+            smp[t] = nP;
+            smp[beads + t] = nV;
+            smp[2 * beads + t] = nFo;
+        }
+        __syncthreads();
+        if (active) {
+            const uint32_t wl = t / L, c = t - wl * L;
+            const float u = u01(rng_draw(P, w0 + wl, n, kRngReverse).x);
+            if (u <= P.reverse_p) {
+                const uint32_t src = wl * L + (L - 1u - c);
+                nP = smp[src];
+                nV = smp[beads + src];
+                nFo = smp[2 * beads + src];
+            }
+        }
+        __syncthreads();
+    }
+    if (active) smp[t] = nP;
+    __syncthreads();
+    const uint32_t wl = active ? t / L : 0u, c = active ? t - wl * L : 0u;
+    const float4* R = smp + wl * L;
+    // each bending triple once, by the thread of its first bead
+    if (active && L >= 3 && c + 2 < L) {
+        const Triple tr = bend_triple(P, f3(R[c]), f3(R[c + 1]), f3(R[c + 2]));
+        smx[t] = make_float4(tr.fi.x, tr.fi.y, tr.fi.z, 0.f);
+        smx[beads + t] = make_float4(tr.fj.x, tr.fj.y, tr.fj.z, 0.f);
+        smx[2 * beads + t] = make_float4(tr.fk.x, tr.fk.y, tr.fk.z, 0.f);
+    }
+    __syncthreads();
+    if (!active) return;
+
+    float3 fs = zero3();
+    if (P.langevin_on) {
+        // langevinKernel (particles_kernel_impl.cuh:859-874), Philox noise in registers
+        const float4 z = normal4(rng_draw(P, i, n, kRngLangevin));
+        const float3 g = make_float3(P.noise_sigma * z.x, P.noise_sigma * z.y, P.dim >= 3 ? P.noise_sigma * z.z : 0.f);
+        float3 fl = zero3() - P.gamma * f3(nV);
+        fl += g;
+        fs = fl;
+    }
+    // bending contributions in the reference's triple order p = c-2, c-1, c
+    if (L >= 3) {
+        if (c >= 2) fs += f3(smx[2 * beads + t - 2]);
+        if (c >= 1 && c + 1 < L) fs += f3(smx[beads + t - 1]);
+        if (c + 2 < L) fs += f3(smx[t]);
+    }
+    bool wt = false;
+    float3 tg = zero3();
+    if (L >= 3) {
+        if (c == 0) {
+            tg = tangent_of(P, f3(R[0]), f3(R[1]));
+            wt = true;
+        } else if (c == L - 1) {
+            if (L > 3) {
+                tg = tangent_of(P, f3(R[L - 2]), f3(R[L - 1]));
+                wt = true;
+            }
+        } else {
+            tg = tangent_of(P, f3(R[c - 1]), f3(R[c + 1]));
+            wt = true;
+        }
+    }
+    if (P.model == NW_MODEL_WCA_WORMS) {
+        const float3 me = f3(R[c]);
+        if (c + 1 < L) wca_bond(P, me, f3(R[c + 1]), fs);
+        if (c > 0) wca_bond(P, me, f3(R[c - 1]), fs);
+        if (c + 1 < L) wca_drive(P, me, f3(R[c + 1]), fs);
+    }
+    S.pos2[out][i] = nP;
+    S.vel2[out][i] = nV;
+    S.force_old[i] = nFo;
+    S.force[i] = make_float4(fs.x, fs.y, fs.z, 0.f);
+    S.tan2[out][i] = wt ? make_float4(tg.x, tg.y, tg.z, 0.f) : S.tan2[in][i];
+    if (!finite3(f3(nP)) || !finite3(fs)) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
+
+    const uint32_t h = bead_hash(P, f3(nP));
+    S.hash2[out][i] = h;
+    const uint32_t slot = atomicAdd(&S.lcount[(uint32_t)(n % 3ull)][h], 1u);
+    if (slot < (uint32_t)CAP) S.lslot[out][(size_t)h * CAP + slot] = i;
+    else atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
+}
+
+template <int CAP, int MAXT>
+__global__ void __launch_bounds__(MAXT) bead_pro_kernel(const DevParams P, const StepBuffers S, uint32_t off, float dt,
+                                                        uint32_t fpb)
+{
+    const unsigned long long n = *S.step_base + off;
+    const uint32_t i = blockIdx.x * fpb * P.L + threadIdx.x;
+    const bool active = threadIdx.x < fpb * P.L && i < P.nb;
+    const float3 fprev = active ? f3(S.force[i]) : zero3();
+    pro_part<CAP>(P, S, n, dt, fpb, active, i, fprev);
+}
+
+template <int CAP, bool kRef>
+__global__ void __launch_bounds__(256) bead_epi_kernel(const DevParams P, const StepBuffers S, uint32_t off)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.nb) return;
+    const unsigned long long n = *S.step_base + off;
+    const float3 pair = list_pair_force<CAP, kRef>(P, S, n, i);
+    float4 F = S.force[i];
+    F.x += pair.x;
+    F.y += pair.y;
+    F.z += pair.z;
+    S.force[i] = F;
+    if (!finite3(f3(F))) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
+}
+
+// epi(n) then pro(n+1): the complete force of update n stays in a register.
+template <int CAP, bool kRef, int MAXT>
+__global__ void __launch_bounds__(MAXT) bead_fused_kernel(const DevParams P, const StepBuffers S, uint32_t off,
+                                                          float dt, uint32_t fpb)
+{
+    const unsigned long long n = *S.step_base + off;
+    const uint32_t i = blockIdx.x * fpb * P.L + threadIdx.x;
+    const bool active = threadIdx.x < fpb * P.L && i < P.nb;
+    float3 Fn = zero3();
+    if (active) {
+        const float3 pair = list_pair_force<CAP, kRef>(P, S, n, i);
+        const float4 F = S.force[i];
+        Fn = make_float3(F.x + pair.x, F.y + pair.y, F.z + pair.z);
+        if (!finite3(Fn)) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
+    }
+    pro_part<CAP>(P, S, n + 1ull, dt, fpb, active, i, Fn);
+}
+
+uint32_t cdiv32(uint64_t a, uint32_t b) { return (uint32_t)((a + b - 1) / b); }
+
+}  // namespace
+
+uint32_t list_filaments_per_block(uint32_t L, uint32_t nf)
+{
+    uint32_t fpb = L >= 256 ? 1u : 256u / L;
+    if (fpb > nf && nf > 0) fpb = nf;
+    return fpb ? fpb : 1u;
+}
+
+static void pro_shape(const DevParams& P, uint32_t& fpb, uint32_t& threads, size_t& smem)
+{
+    fpb = list_filaments_per_block(P.L, P.nf);
+    const uint32_t beads = fpb * P.L;
+    threads = (beads + 31u) & ~31u;
+    smem = pro_smem(beads, P.reverse_on != 0);
+}
+
+uint64_t launch_bead_pro(const DevParams& P, const StepBuffers& B, uint32_t off, float dt, cudaStream_t s)
+{
+    if (P.nb == 0) return 0;
+    uint32_t fpb, threads;
+    size_t smem;
+    pro_shape(P, fpb, threads, smem);
+    const uint32_t blocks = cdiv32(P.nf, fpb);
+    const bool big = threads > 256;  // filaments longer than 256 beads: one per block, up to 1024 threads
+    if (B.cap == 16) {
+        if (big) bead_pro_kernel<16, 1024><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb);
+        else bead_pro_kernel<16, 256><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb);
+    } else {
+        if (big) bead_pro_kernel<8, 1024><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb);
+        else bead_pro_kernel<8, 256><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb);
+    }
+    return 1;
+}
+
+uint64_t launch_bead_epi(const DevParams& P, const StepBuffers& B, uint32_t off, cudaStream_t s)
+{
+    if (P.nb == 0) return 0;
+    const uint32_t blocks = cdiv32(P.nb, 256);
+    const bool ref = P.model == NW_MODEL_REF_DEM;
+    if (B.cap == 16) {
+        if (ref) bead_epi_kernel<16, true><<<blocks, 256, 0, s>>>(P, B, off);
+        else bead_epi_kernel<16, false><<<blocks, 256, 0, s>>>(P, B, off);
+    } else {
+        if (ref) bead_epi_kernel<8, true><<<blocks, 256, 0, s>>>(P, B, off);
+        else bead_epi_kernel<8, false><<<blocks, 256, 0, s>>>(P, B, off);
+    }
+    return 1;
+}
+
+uint64_t launch_bead_fused(const DevParams& P, const StepBuffers& B, uint32_t off, float dt, cudaStream_t s)
+{
+    if (P.nb == 0) return 0;
+    uint32_t fpb, threads;
+    size_t smem;
+    pro_shape(P, fpb, threads, smem);
+    const uint32_t blocks = cdiv32(P.nf, fpb);
+    const bool ref = P.model == NW_MODEL_REF_DEM;
+    const bool big = threads > 256;
+#define NW_FUSED(CAPV, REFV)                                                                        \
+    do {                                                                                            \
+        if (big) bead_fused_kernel<CAPV, REFV, 1024><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb); \
+        else bead_fused_kernel<CAPV, REFV, 256><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb);      \
+    } while (0)
+    if (B.cap == 16) {
+        if (ref) NW_FUSED(16, true);
+        else NW_FUSED(16, false);
+    } else {
+        if (ref) NW_FUSED(8, true);
+        else NW_FUSED(8, false);
+    }
+#undef NW_FUSED
+    return 1;
+}
+
+}  // namespace nw

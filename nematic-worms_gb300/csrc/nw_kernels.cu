@@ -238,23 +238,37 @@ __global__ void __launch_bounds__(256) pair_wca_kernel(const DevParams P, const 
     if (!finite3(f3(F))) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
 }
 
+// Particle id -> its velocity / position slot: beads in the current bead
+// buffer, solvent in the solvent arrays.
+__device__ __forceinline__ float4* vel_slot(const StepBuffers& S, uint32_t nb, uint32_t cur, uint32_t id)
+{
+    return id < nb ? S.vel2[cur] + id : S.svel + (id - nb);
+}
+__device__ __forceinline__ float4* pos_slot(const StepBuffers& S, uint32_t nb, uint32_t cur, uint32_t id)
+{
+    return id < nb ? S.pos2[cur] + id : S.spos + (id - nb);
+}
+
 __global__ void __launch_bounds__(256) srd_hash_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
-                                                       int shift_from_step, float3 shift)
+                                                       int shift_from_step, float3 shift, uint32_t buf_sel)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.ntotal) return;
-    if (shift_from_step) shift = srd_shift_of(P, *S.step_base + step_off);
-    const uint32_t h = srd_hash(P, f3(S.pos[i]), shift);
+    const unsigned long long step = *S.step_base + step_off;
+    if (shift_from_step) shift = srd_shift_of(P, step);
+    const uint32_t cur = buf_sel < 2u ? buf_sel : (uint32_t)(step & 1ull);
+    const uint32_t h = srd_hash(P, f3(*pos_slot(S, P.nb, cur, i)), shift);
     S.srd_hash[i] = h;
     S.srd_slot[i] = count_into_cell(S.srd_count, h);
 }
 
 __global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
-                                                          float dt_srd)
+                                                          float dt_srd, uint32_t buf_sel)
 {
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= P.srd_ncells) return;
     const unsigned long long step = *S.step_base + step_off;
+    const uint32_t cur = buf_sel < 2u ? buf_sel : (uint32_t)(step & 1ull);
     const uint32_t lo = S.srd_offset[c], hi = S.srd_offset[c + 1];
     const uint32_t n = hi - lo;
     float3 u = zero3();
@@ -287,20 +301,20 @@ __global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, con
         if (P.srd_thermo == NW_SRD_THERMO_REF_LAB) {
             float E = 0.f;
             for (uint32_t k = 0; k < n; ++k) {
-                const float4 V = S.vel[member(k)];
+                const float4 V = *vel_slot(S, P.nb, cur, member(k));
                 const float3 v = f3(V);
                 E += (0.5f * V.w) * dot3(v, v);
             }
             const float lam = sqrtf(P.srd_kT / E);
             for (uint32_t k = 0; k < n; ++k) {
-                const uint32_t id = member(k);
-                const float4 V = S.vel[id];
-                S.vel[id] = make_float4(lam * V.x, lam * V.y, lam * V.z, V.w);
+                float4* vp = vel_slot(S, P.nb, cur, member(k));
+                const float4 V = *vp;
+                *vp = make_float4(lam * V.x, lam * V.y, lam * V.z, V.w);
             }
         }
         float M = 0.f;
         for (uint32_t k = 0; k < n; ++k) {
-            const float4 V = S.vel[member(k)];
+            const float4 V = *vel_slot(S, P.nb, cur, member(k));
             u += V.w * f3(V);
             M += V.w;
         }
@@ -316,11 +330,12 @@ __global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, con
         for (uint32_t k = 0; k < n; ++k) {
             const uint32_t id = member(k);
             if (id < P.nb && !P.srd_rotate_beads) continue;
-            const float4 V = S.vel[id];
+            float4* vp = vel_slot(S, P.nb, cur, id);
+            const float4 V = *vp;
             const float3 d = f3(V) - u;
             const float rx = d.x * ca - d.y * sa;
             const float ry = d.x * sa + d.y * ca;
-            S.vel[id] = make_float4(u.x + rx, u.y + ry, u.z + d.z, V.w);
+            *vp = make_float4(u.x + rx, u.y + ry, u.z + d.z, V.w);
             ke += (0.5f * V.w) * (rx * rx + ry * ry);
             ++nrot;
         }
@@ -329,21 +344,24 @@ __global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, con
             for (uint32_t k = 0; k < n; ++k) {
                 const uint32_t id = member(k);
                 if (id < P.nb && !P.srd_rotate_beads) continue;
-                const float4 V = S.vel[id];
-                S.vel[id] = make_float4(u.x + lam * (V.x - u.x), u.y + lam * (V.y - u.y), V.z, V.w);
+                float4* vp = vel_slot(S, P.nb, cur, id);
+                const float4 V = *vp;
+                *vp = make_float4(u.x + lam * (V.x - u.x), u.y + lam * (V.y - u.y), V.z, V.w);
             }
         }
         for (uint32_t k = 0; k < n; ++k) {
             const uint32_t id = member(k);
             if (id < P.nb) continue;
-            const float4 P4 = S.pos[id];
-            const float4 V4 = S.vel[id];
+            float4* pp = S.spos + (id - P.nb);
+            float4* vp = S.svel + (id - P.nb);
+            const float4 P4 = *pp;
+            const float4 V4 = *vp;
             float3 p = f3(P4), v = f3(V4);
             const float3 dr = dt_srd * v;
             p += dr;
             apply_boundaries(P, p, v, dr, 0.0f);
-            S.pos[id] = make_float4(p.x, p.y, p.z, P4.w);
-            S.vel[id] = make_float4(v.x, v.y, v.z, V4.w);
+            *pp = make_float4(p.x, p.y, p.z, P4.w);
+            *vp = make_float4(v.x, v.y, v.z, V4.w);
         }
     }
     S.srd_mean[c] = make_float4(u.x, u.y, u.z, 0.f);

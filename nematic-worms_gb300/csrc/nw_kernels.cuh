@@ -25,8 +25,20 @@ constexpr uint32_t kPairCap = 1024;   // members scanned per neighbour cell
 constexpr uint32_t kSrdLocal = 32;    // SRD members kept in registers
 
 struct StepBuffers {
+    // Bead state.  pos2/vel2/tan2/hash2 are double buffers: the cell-list path
+    // writes update n into [n & 1] while other blocks still read [(n-1) & 1];
+    // the sorted path updates in place, with both entries naming one array.
+    float4 *pos2[2], *vel2[2], *tan2[2];
+    uint32_t* hash2[2];
+    // in-place views of the sorted path (= pos2[0], ...)
     float4 *pos, *vel, *force, *force_old, *tangent;
     uint32_t *hash, *slot, *tmp_index, *sorted_index, *sorted_hash;
+    // solvent state (particle nb + k is solvent k)
+    float4 *spos, *svel;
+    // capped per-cell bead lists of the cell-list path: counts of update n in
+    // lcount[n % 3], members in lslot[n & 1][cell * cap + slot]
+    uint32_t *lcount[3], *lslot[2];
+    uint32_t cap;
     uint32_t *cell_count, *cell_offset, *cell_start, *cell_end, *chunk_count;
     float4 *sorted_pos, *sorted_vel, *sorted_tan;
     uint32_t *srd_hash, *srd_slot, *srd_tmp, *srd_sorted_index;
@@ -376,7 +388,7 @@ __device__ __forceinline__ float3 srd_shift_of(const DevParams& P, unsigned long
 
 // calcHashD(srd = true) over beads and solvent + counting-sort slot.
 __global__ void __launch_bounds__(256) srd_hash_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
-                                                       int shift_from_step, float3 shift);
+                                                       int shift_from_step, float3 shift, uint32_t buf_sel);
 
 // One SRD cell per thread: members in stable (index) order, then the
 // reference's isokinetic thermostat (particles_kernel_impl.cuh:605-637) or
@@ -384,7 +396,7 @@ __global__ void __launch_bounds__(256) srd_hash_kernel(const DevParams P, const 
 // (v - u) (:640-691), the relative-velocity thermostat when selected, and the
 // solvent's ballistic streaming by dt_srd (solvent_integrator, :145-205).
 __global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
-                                                          float dt_srd);
+                                                          float dt_srd, uint32_t buf_sel);
 
 __global__ void advance_step_kernel(unsigned long long* step_base, unsigned long long k);
 

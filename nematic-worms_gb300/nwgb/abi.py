@@ -38,6 +38,7 @@ NW_MODEL_REF_DEM = 1
 NW_PERIODIC, NW_WALL, NW_WALL_NO_SLIP = 0, 1, 2
 NW_HASH_MODULO, NW_HASH_MASK = 0, 1
 NW_SRD_THERMO_NONE, NW_SRD_THERMO_REF_LAB, NW_SRD_THERMO_CELL_REL = 0, 1, 2
+NW_STRATEGY_AUTO, NW_STRATEGY_SORTED, NW_STRATEGY_CELL_LISTS = 0, 1, 2
 
 NW_POSITION = 0
 NW_VELOCITY = 1
@@ -109,7 +110,9 @@ class NwConfig(C.Structure):
         ("srd_thermostat", _i32),
         ("seed", C.c_uint64),
         ("dt", _f32),
-        ("reserved", _u32 * 7),
+        ("strategy", _i32),
+        ("cell_capacity", _u32),
+        ("reserved", _u32 * 5),
     ]
 
     def copy(self) -> "NwConfig":

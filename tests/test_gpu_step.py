@@ -88,11 +88,16 @@ def run_oracle(orc, cfg, pos, vel, tan, nsteps=1, prec=32):
 
 
 CASES = ["wca", "wca_srd", "wca_reverse", "ref", "ref_srd", "ref_walls"]
+STRATEGIES = [abi.NW_STRATEGY_CELL_LISTS, abi.NW_STRATEGY_SORTED]
+# launches of one update: (bead step, SRD collision) + the step counter
+LAUNCHES = {abi.NW_STRATEGY_CELL_LISTS: (2, 5), abi.NW_STRATEGY_SORTED: (6, 5)}
 
 
+@pytest.mark.parametrize("strategy", STRATEGIES)
 @pytest.mark.parametrize("kind", CASES)
-def test_one_step_matches_oracle(lib, orc, kind):
+def test_one_step_matches_oracle(lib, orc, kind, strategy):
     cfg, pos, vel, tan = make_case(kind, lib)
+    cfg.strategy = strategy
     g = run_gpu(cfg, pos, vel, tan)
     o = run_oracle(orc, cfg, pos, vel, tan, 1, 32)
     o64 = run_oracle(orc, cfg, pos, vel, tan, 1, 64)
@@ -108,23 +113,43 @@ def test_one_step_matches_oracle(lib, orc, kind):
         assert rel_err(a, b) < TOL32, (k, rel_err(a, b))
         b64 = o64[k][:nb] if k in ("pos", "vel") else o64[k]
         assert rel_err(a, b64) < TOL64, (k, "fp64", rel_err(a, b64))
+    bead, srd = LAUNCHES[strategy]
     if cfg.srd_enabled:  # solvent after the collision of step 0
         assert rel_err(g["pos"][nb:], o["pos"][nb:]) < TOL32
         assert rel_err(g["vel"][nb:], o["vel"][nb:]) < TOL32
-        assert g["launches"] == 6 + 5 + 1  # bead step, SRD collision, step counter
+        assert g["launches"] == bead + srd + 1
     else:
-        assert g["launches"] == 6 + 1
+        assert g["launches"] == bead + 1
 
 
+@pytest.mark.parametrize("strategy", STRATEGIES)
 @pytest.mark.parametrize("kind", ["wca", "ref_srd"])
-def test_graph_replay_is_bit_identical_to_direct_launches(lib, kind):
+def test_graph_replay_is_bit_identical_to_direct_launches(lib, kind, strategy):
     cfg, pos, vel, tan = make_case(kind, lib)
+    cfg.strategy = strategy
     a = run_gpu(cfg, pos, vel, tan, nsteps=12, graphs=True)
     b = run_gpu(cfg, pos, vel, tan, nsteps=12, graphs=False)
     c = run_gpu(cfg, pos, vel, tan, nsteps=12, graphs=True)
     for k in ("pos", "vel", "force", "tangent", "sorted_index"):
         assert np.array_equal(a[k], b[k]), k
         assert np.array_equal(a[k], c[k]), k  # run twice: no races
+
+
+@pytest.mark.parametrize("kind", ["wca", "wca_srd", "ref"])
+def test_strategies_agree(lib, kind):
+    """Cell lists visit each cell's beads in index order, as the sorted
+    arrays do: both strategies give the same cell assignment and sort order
+    and the same trajectory up to FP32 contraction differences of the two
+    kernel codes."""
+    cfg, pos, vel, tan = make_case(kind, lib)
+    out = []
+    for strategy in STRATEGIES:
+        cfg.strategy = strategy
+        out.append(run_gpu(cfg, pos, vel, tan, nsteps=15, graphs=True))
+    for k in ("hash", "sorted_index", "cell_start"):
+        assert np.array_equal(out[0][k], out[1][k]), k
+    for k in ("pos", "vel", "force", "force_old", "tangent"):
+        assert rel_err(out[0][k], out[1][k]) < 1e-5, k
 
 
 @pytest.mark.parametrize("kind", ["wca", "wca_srd", "ref"])
