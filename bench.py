@@ -58,10 +58,14 @@ def alg_bytes(name: str, cfg) -> float:
         "filament_pass": 152.0 * nb,
         # count read, offset/start/end written, count reset
         "scan_cells": 20.0 * C,
-        "srd_scan_cells": 20.0 * Cs,
+        # bead and solvent bucket counts read, offsets written, counts reset
+        "srd_scan_cells": 24.0 * Cs,
+        "srd_chunk_sum": 8.0 * Cs,
+        "chunk_sum": 4.0 * C,
         # hash + slot read, index written
         "scatter": 12.0 * nb,
-        "srd_scatter": 12.0 * nt,
+        # hash + slot read, bucket offset read, bucket entry written
+        "srd_scatter": 16.0 * nt,
         # bucket index + hash + position read; sorted index, hash, position written
         "stable_gather": 48.0 * nb,
         # sorted position + index read, force read-modify-write, cell bounds read
@@ -76,8 +80,9 @@ def alg_bytes(name: str, cfg) -> float:
         "bead_fused": 156.0 * nb + 12.0 * C,
         # position read, hash + slot written
         "srd_hash": 24.0 * nt,
-        # member index + velocity read/write; solvent position read/write; cell offsets + mean
-        "srd_collide": 36.0 * nt + 32.0 * ns + 20.0 * Cs,
+        # bucket entry + velocity read, stable index written; bead velocity written in place;
+        # solvent position read, position + velocity written in cell order; offsets, bounds, mean
+        "srd_collide": 24.0 * nt + 16.0 * nb + 48.0 * ns + 32.0 * Cs,
         "advance_step": 8.0,
     }
     return table.get(name, 0.0)

@@ -135,15 +135,19 @@ uint64_t enqueue_srd(const DevParams& P, const StepBuffers& B, uint32_t srd_nchu
     NW_MARK("srd_hash");
     srd_hash_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(P, B, step_off, shift_from_step, shift, buf_sel);
     NW_MARK("srd_chunk_sum");
-    chunk_sum_kernel<<<srd_nchunks, 512, 0, s>>>(B.srd_count, P.srd_ncells, B.srd_chunk);
+    chunk_sum_kernel<<<srd_nchunks, 512, 0, s>>>(B.srd_bcount, P.srd_ncells, B.srd_bchunk);
+    chunk_sum_kernel<<<srd_nchunks, 512, 0, s>>>(B.srd_scount, P.srd_ncells, B.srd_schunk);
     NW_MARK("srd_scan_cells");
-    scan_cells_kernel<true><<<srd_nchunks, 512, 0, s>>>(B.srd_count, B.srd_chunk, P.srd_ncells, B.srd_offset,
-                                                        B.srd_start, B.srd_end);
+    scan_cells_kernel<false><<<srd_nchunks, 512, 0, s>>>(B.srd_bcount, B.srd_bchunk, P.srd_ncells, B.srd_boff,
+                                                         nullptr, nullptr);
+    scan_cells_kernel<false><<<srd_nchunks, 512, 0, s>>>(B.srd_scount, B.srd_schunk, P.srd_ncells, B.srd_soff,
+                                                         nullptr, nullptr);
     NW_MARK("srd_scatter");
-    scatter_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(B.srd_hash, B.srd_slot, B.srd_offset, B.srd_tmp, P.ntotal);
+    srd_scatter_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(P, B);
     NW_MARK("srd_collide");
     srd_collide_kernel<<<cdiv(P.srd_ncells, 256), 256, 0, s>>>(P, B, step_off, dt_srd, buf_sel);
-    return 5;
+    srd_flip_kernel<<<1, 1, 0, s>>>(B.scur);
+    return 8;
 }
 
 // Histogram of bead hashes (the counting sort's first pass, for the sorted
@@ -181,6 +185,7 @@ struct nw_system {
     bool use_graphs = true;
     bool lists_dirty = false;  // list counters must be cleared before the next update
     uint64_t sorted_for = ~0ull;  // step whose sorted order / cell bounds are in the sort buffers
+    uint32_t scur = 0;            // solvent buffer holding the current solvent (mirror of *B.scur)
     std::vector<GraphEntry> graphs;
     uint64_t last_launches = 0;
     std::vector<void*> allocs;
@@ -234,6 +239,18 @@ nw_status cuda_status(cudaError_t e)
 
 // Bead buffer holding the state after the last update.
 uint32_t cur_buffer(const nw_system* s) { return s->lists ? (uint32_t)((s->step + 1ull) & 1ull) : 0u; }
+
+// Parity of the number of SRD collisions in updates [first, first + nsteps):
+// each collision moves the solvent to the other buffer.
+uint32_t collision_parity(const nw_system* s, uint64_t first, int nsteps)
+{
+    if (!s->cfg.srd_enabled || nsteps <= 0) return 0u;
+    const uint64_t gap = s->cfg.srd_gap ? s->cfg.srd_gap : 1u;
+    const uint64_t last = first + (uint64_t)nsteps - 1ull;
+    const uint64_t upto_last = last / gap + 1ull;            // multiples of gap in [0, last]
+    const uint64_t before = first ? (first - 1ull) / gap + 1ull : 0ull;  // in [0, first)
+    return (uint32_t)((upto_last - before) & 1ull);
+}
 
 // Clear the list counters when the step counter changed under them.
 cudaError_t clean_lists(nw_system* s)
@@ -322,8 +339,8 @@ nw_status transfer(nw_system* s, int array, void* host, uint32_t start, uint32_t
     size_t elem = 16;
     size_t nbead = s->nb, ntot = s->nb;
     switch (array) {
-    case NW_POSITION: bead_ptr = B.pos2[cur]; solv_ptr = B.spos; ntot = s->ntotal; break;
-    case NW_VELOCITY: bead_ptr = B.vel2[cur]; solv_ptr = B.svel; ntot = s->ntotal; break;
+    case NW_POSITION: bead_ptr = B.pos2[cur]; solv_ptr = B.spos2[s->scur]; ntot = s->ntotal; break;
+    case NW_VELOCITY: bead_ptr = B.vel2[cur]; solv_ptr = B.svel2[s->scur]; ntot = s->ntotal; break;
     case NW_TANGENT: bead_ptr = B.tan2[cur]; break;
     case NW_FORCE: bead_ptr = B.force; break;
     case NW_FORCE_OLD: bead_ptr = B.force_old; break;
@@ -433,8 +450,11 @@ nw_status nw_create(const NwConfig* cfg, nw_system** out)
     B.hash = B.hash2[0];
     A(alloc_n(s, &B.force, nb));
     A(alloc_n(s, &B.force_old, nb));
-    A(alloc_n(s, &B.spos, ns));
-    A(alloc_n(s, &B.svel, ns));
+    for (int k = 0; k < 2; ++k) {
+        A(alloc_n(s, &B.spos2[k], ns));
+        A(alloc_n(s, &B.svel2[k], ns));
+    }
+    A(alloc_n(s, &B.scur, 4));
     A(alloc_n(s, &B.slot, nb));
     A(alloc_n(s, &B.tmp_index, nb));
     A(alloc_n(s, &B.sorted_index, nb));
@@ -457,13 +477,17 @@ nw_status nw_create(const NwConfig* cfg, nw_system** out)
         const size_t Cs = s->srd_ncells, nt = s->ntotal;
         A(alloc_n(s, &B.srd_hash, nt));
         A(alloc_n(s, &B.srd_slot, nt));
-        A(alloc_n(s, &B.srd_tmp, nt));
+        A(alloc_n(s, &B.srd_btmp, nb));
+        A(alloc_n(s, &B.srd_stmp, ns));
         A(alloc_n(s, &B.srd_sorted_index, nt));
-        A(alloc_n(s, &B.srd_count, Cs + 8));
-        A(alloc_n(s, &B.srd_offset, Cs + 8));
+        A(alloc_n(s, &B.srd_bcount, Cs + 8));
+        A(alloc_n(s, &B.srd_scount, Cs + 8));
+        A(alloc_n(s, &B.srd_boff, Cs + 8));
+        A(alloc_n(s, &B.srd_soff, Cs + 8));
         A(alloc_n(s, &B.srd_start, Cs + 8));
         A(alloc_n(s, &B.srd_end, Cs + 8));
-        A(alloc_n(s, &B.srd_chunk, (size_t)s->srd_nchunks + 1));
+        A(alloc_n(s, &B.srd_bchunk, (size_t)s->srd_nchunks + 1));
+        A(alloc_n(s, &B.srd_schunk, (size_t)s->srd_nchunks + 1));
         A(alloc_n(s, &B.srd_mean, Cs));
     }
     A(alloc_n(s, &B.err, 4));
@@ -486,8 +510,11 @@ nw_status nw_create(const NwConfig* cfg, nw_system** out)
     }
     Z(B.force, nb * 16);
     Z(B.force_old, nb * 16);
-    Z(B.spos, ns * 16);
-    Z(B.svel, ns * 16);
+    for (int k = 0; k < 2; ++k) {
+        Z(B.spos2[k], ns * 16);
+        Z(B.svel2[k], ns * 16);
+    }
+    Z(B.scur, 4);
     Z(B.cell_count, (C + 8) * 4);
     Z(B.chunk_count, ((size_t)s->nchunks + 1) * 4);
     Z(B.cell_start, (C + 8) * 4, 0xff);
@@ -495,8 +522,8 @@ nw_status nw_create(const NwConfig* cfg, nw_system** out)
     if (s->lists)
         for (int k = 0; k < 3; ++k) Z(B.lcount[k], (C + 8) * 4);
     if (cfg->srd_enabled) {
-        Z(B.srd_count, ((size_t)s->srd_ncells + 8) * 4);
-        Z(B.srd_chunk, ((size_t)s->srd_nchunks + 1) * 4);
+        Z(B.srd_bcount, ((size_t)s->srd_ncells + 8) * 4);
+        Z(B.srd_scount, ((size_t)s->srd_ncells + 8) * 4);
         Z(B.srd_mean, (size_t)s->srd_ncells * 16);
     }
     Z(B.err, 16);
@@ -648,6 +675,7 @@ nw_status nw_step(nw_system* s, int nsteps, float dt)
         e = cudaGetLastError();
     }
     if (e != cudaSuccess) return cuda_status(e);
+    s->scur ^= collision_parity(s, s->step, nsteps);
     s->step += (uint64_t)nsteps;
     return NW_OK;
 }
@@ -733,6 +761,7 @@ nw_status nw_srd_collide(nw_system* s, float dt_srd, const float shift[3])
     const DevParams P = make_dev_params(s->cfg, s->cfg.dt);
     s->last_launches = enqueue_srd(P, s->B, s->srd_nchunks, 0u, dt_srd, 0, make_float3(shift[0], shift[1], shift[2]),
                                    s->stream, nullptr, cur_buffer(s));
+    s->scur ^= 1u;
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     return cuda_status(e);
@@ -830,6 +859,7 @@ nw_status nw_profile_steps(nw_system* s, int nsteps, float dt, NwKernelTime* out
         prof.clear();
         return cuda_status(e);
     }
+    s->scur ^= collision_parity(s, s->step, nsteps);
     s->step += (uint64_t)nsteps;
     int n = 0;
     for (size_t k = 0; k + 1 < prof.events.size(); ++k) {

@@ -238,30 +238,56 @@ __global__ void __launch_bounds__(256) pair_wca_kernel(const DevParams P, const 
     if (!finite3(f3(F))) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
 }
 
-// Particle id -> its velocity / position slot: beads in the current bead
-// buffer, solvent in the solvent arrays.
-__device__ __forceinline__ float4* vel_slot(const StepBuffers& S, uint32_t nb, uint32_t cur, uint32_t id)
-{
-    return id < nb ? S.vel2[cur] + id : S.svel + (id - nb);
-}
-__device__ __forceinline__ float4* pos_slot(const StepBuffers& S, uint32_t nb, uint32_t cur, uint32_t id)
-{
-    return id < nb ? S.pos2[cur] + id : S.spos + (id - nb);
-}
-
+// SRD cell hash of every particle (beads from the current bead buffer,
+// solvent from the current solvent buffer) and its slot in its cell's bead
+// or solvent bucket.  Lanes of a warp that share a bucket take consecutive
+// slots from one atomic (the solvent is stored in cell order, so a warp's
+// particles fall into few cells).
 __global__ void __launch_bounds__(256) srd_hash_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
                                                        int shift_from_step, float3 shift, uint32_t buf_sel)
 {
+    // every lane of the warp takes part in the match (blockDim is a multiple of 32)
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.ntotal) return;
+    const bool valid = i < P.ntotal;
     const unsigned long long step = *S.step_base + step_off;
     if (shift_from_step) shift = srd_shift_of(P, step);
     const uint32_t cur = buf_sel < 2u ? buf_sel : (uint32_t)(step & 1ull);
-    const uint32_t h = srd_hash(P, f3(*pos_slot(S, P.nb, cur, i)), shift);
-    S.srd_hash[i] = h;
-    S.srd_slot[i] = count_into_cell(S.srd_count, h);
+    const bool bead = i < P.nb;
+    uint32_t h = 0, key = 0xffffffffu;  // no cell hash reaches 2^31 - 1 with the bead bit set
+    if (valid) {
+        const float4 p4 = bead ? S.pos2[cur][i] : S.spos2[*S.scur][i - P.nb];
+        h = srd_hash(P, f3(p4), shift);
+        S.srd_hash[i] = h;
+        key = h | (bead ? 0x80000000u : 0u);
+    }
+    const uint32_t peers = __match_any_sync(0xffffffffu, key);
+    const int lane = (int)(threadIdx.x & 31u);
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (valid && lane == leader) base = atomicAdd(bead ? &S.srd_bcount[h] : &S.srd_scount[h], (uint32_t)__popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (valid) S.srd_slot[i] = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
 }
 
+// Bucket every particle: beads by bead index, solvent by solvent index.
+__global__ void __launch_bounds__(256) srd_scatter_kernel(const DevParams P, const StepBuffers S)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.ntotal) return;
+    const uint32_t h = S.srd_hash[i], slot = S.srd_slot[i];
+    if (i < P.nb) S.srd_btmp[S.srd_boff[h] + slot] = i;
+    else S.srd_stmp[S.srd_soff[h] + slot] = i - P.nb;
+}
+
+// One SRD cell per thread.  Members in the stable (cell, index) order: the
+// cell's beads, then its solvent.  The reference's isokinetic scaling
+// (particles_kernel_impl.cuh:605-637) or none, the mass-weighted cell mean
+// (:560-594), the +/- alpha rotation of (v - u) (:640-691), the
+// relative-velocity thermostat when selected, and the solvent's ballistic
+// streaming by dt_srd (solvent_integrator, :145-205).  Velocities are read
+// once per pass from the pre-collision buffers and written once: beads in
+// place, solvent to the other solvent buffer at its new position in cell
+// order.
 __global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
                                                           float dt_srd, uint32_t buf_sel)
 {
@@ -269,18 +295,27 @@ __global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, con
     if (c >= P.srd_ncells) return;
     const unsigned long long step = *S.step_base + step_off;
     const uint32_t cur = buf_sel < 2u ? buf_sel : (uint32_t)(step & 1ull);
-    const uint32_t lo = S.srd_offset[c], hi = S.srd_offset[c + 1];
-    const uint32_t n = hi - lo;
+    const uint32_t a = *S.scur;
+    const float4* __restrict__ sv_old = S.svel2[a];
+    const float4* __restrict__ sp_old = S.spos2[a];
+    float4* __restrict__ sv_new = S.svel2[a ^ 1u];
+    float4* __restrict__ sp_new = S.spos2[a ^ 1u];
+    float4* __restrict__ bvel = S.vel2[cur];
+    const uint32_t b0 = S.srd_boff[c], b1 = S.srd_boff[c + 1];
+    const uint32_t s0 = S.srd_soff[c], s1 = S.srd_soff[c + 1];
+    const uint32_t nbc = b1 - b0, nsc = s1 - s0, n = nbc + nsc;
+    const uint32_t start = b0 + s0;  // particles before this cell in the stable order
+    S.srd_start[c] = n ? start : kEmpty;
+    S.srd_end[c] = n ? start + n : kEmpty;
     float3 u = zero3();
     if (n > 0) {
-        // stable member order
+        // members in stable order: ids < nb are beads, nb + k is solvent k
         uint32_t ids[kSrdLocal];
         const bool local = n <= kSrdLocal;
-        const bool exact = n <= kStableCap;
-        if (!exact) atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
+        if (n > kStableCap) atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
         if (local) {
             for (uint32_t k = 0; k < n; ++k) {
-                const uint32_t x = S.srd_tmp[lo + k];
+                const uint32_t x = k < nbc ? S.srd_btmp[b0 + k] : P.nb + S.srd_stmp[s0 + (k - nbc)];
                 uint32_t m = k;
                 while (m > 0 && ids[m - 1] > x) {
                     ids[m] = ids[m - 1];
@@ -288,34 +323,38 @@ __global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, con
                 }
                 ids[m] = x;
             }
-            for (uint32_t k = 0; k < n; ++k) S.srd_sorted_index[lo + k] = ids[k];
+            for (uint32_t k = 0; k < n; ++k) S.srd_sorted_index[start + k] = ids[k];
         } else {
-            for (uint32_t q = lo; q < hi; ++q) {
-                const uint32_t x = S.srd_tmp[q];
-                const uint32_t rnk = exact ? bucket_rank(S.srd_tmp, lo, hi, x, q, S.err) : q - lo;
-                S.srd_sorted_index[lo + rnk] = x;
+            for (uint32_t q = b0; q < b1; ++q) {
+                const uint32_t x = S.srd_btmp[q];
+                const uint32_t r = nbc <= kStableCap ? bucket_rank(S.srd_btmp, b0, b1, x, q, S.err) : q - b0;
+                S.srd_sorted_index[start + r] = x;
+            }
+            for (uint32_t q = s0; q < s1; ++q) {
+                const uint32_t x = S.srd_stmp[q];
+                const uint32_t r = nsc <= kStableCap ? bucket_rank(S.srd_stmp, s0, s1, x, q, S.err) : q - s0;
+                S.srd_sorted_index[start + nbc + r] = P.nb + x;
             }
         }
-        // after this point members are read back in stable order
-        auto member = [&](uint32_t k) -> uint32_t { return local ? ids[k] : S.srd_sorted_index[lo + k]; };
-        if (P.srd_thermo == NW_SRD_THERMO_REF_LAB) {
+        auto member = [&](uint32_t k) -> uint32_t { return local ? ids[k] : S.srd_sorted_index[start + k]; };
+        auto vel_of = [&](uint32_t id) -> float4 { return id < P.nb ? bvel[id] : sv_old[id - P.nb]; };
+        // reference isokinetic rule: lambda scales every member before the mean
+        float lam1 = 1.0f;
+        const bool lab = P.srd_thermo == NW_SRD_THERMO_REF_LAB;
+        if (lab) {
             float E = 0.f;
             for (uint32_t k = 0; k < n; ++k) {
-                const float4 V = *vel_slot(S, P.nb, cur, member(k));
+                const float4 V = vel_of(member(k));
                 const float3 v = f3(V);
                 E += (0.5f * V.w) * dot3(v, v);
             }
-            const float lam = sqrtf(P.srd_kT / E);
-            for (uint32_t k = 0; k < n; ++k) {
-                float4* vp = vel_slot(S, P.nb, cur, member(k));
-                const float4 V = *vp;
-                *vp = make_float4(lam * V.x, lam * V.y, lam * V.z, V.w);
-            }
+            lam1 = sqrtf(P.srd_kT / E);
         }
+        auto scaled = [&](float4 V) -> float3 { return lab ? make_float3(lam1 * V.x, lam1 * V.y, lam1 * V.z) : f3(V); };
         float M = 0.f;
         for (uint32_t k = 0; k < n; ++k) {
-            const float4 V = *vel_slot(S, P.nb, cur, member(k));
-            u += V.w * f3(V);
+            const float4 V = vel_of(member(k));
+            u += V.w * scaled(V);
             M += V.w;
         }
         if (M > 0.f) {
@@ -325,47 +364,58 @@ __global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, con
         const int sign = 2 * (int)(u01(rng_draw(P, c, step, kRngSrdRot).x) > 0.5f) - 1;
         const float ang = (float)sign * P.srd_alpha;
         const float sa = sinf(ang), ca = cosf(ang);
-        uint32_t nrot = 0;
-        float ke = 0.f;
-        for (uint32_t k = 0; k < n; ++k) {
-            const uint32_t id = member(k);
-            if (id < P.nb && !P.srd_rotate_beads) continue;
-            float4* vp = vel_slot(S, P.nb, cur, id);
-            const float4 V = *vp;
-            const float3 d = f3(V) - u;
-            const float rx = d.x * ca - d.y * sa;
-            const float ry = d.x * sa + d.y * ca;
-            *vp = make_float4(u.x + rx, u.y + ry, u.z + d.z, V.w);
-            ke += (0.5f * V.w) * (rx * rx + ry * ry);
-            ++nrot;
-        }
-        if (P.srd_thermo == NW_SRD_THERMO_CELL_REL && nrot >= 2u && ke > 0.f) {
-            const float lam = sqrtf(((float)(nrot - 1u) * P.srd_kT) / ke);
+        const bool rel = P.srd_thermo == NW_SRD_THERMO_CELL_REL;
+        float lam2 = 1.0f;
+        bool scale2 = false;
+        if (rel) {
+            uint32_t nrot = 0;
+            float ke = 0.f;
             for (uint32_t k = 0; k < n; ++k) {
                 const uint32_t id = member(k);
                 if (id < P.nb && !P.srd_rotate_beads) continue;
-                float4* vp = vel_slot(S, P.nb, cur, id);
-                const float4 V = *vp;
-                *vp = make_float4(u.x + lam * (V.x - u.x), u.y + lam * (V.y - u.y), V.z, V.w);
+                const float4 V = vel_of(id);
+                const float3 d = scaled(V) - u;
+                const float rx = d.x * ca - d.y * sa;
+                const float ry = d.x * sa + d.y * ca;
+                ke += (0.5f * V.w) * (rx * rx + ry * ry);
+                ++nrot;
+            }
+            if (nrot >= 2u && ke > 0.f) {
+                lam2 = sqrtf(((float)(nrot - 1u) * P.srd_kT) / ke);
+                scale2 = true;
             }
         }
         for (uint32_t k = 0; k < n; ++k) {
             const uint32_t id = member(k);
-            if (id < P.nb) continue;
-            float4* pp = S.spos + (id - P.nb);
-            float4* vp = S.svel + (id - P.nb);
-            const float4 P4 = *pp;
-            const float4 V4 = *vp;
-            float3 p = f3(P4), v = f3(V4);
-            const float3 dr = dt_srd * v;
-            p += dr;
-            apply_boundaries(P, p, v, dr, 0.0f);
-            *pp = make_float4(p.x, p.y, p.z, P4.w);
-            *vp = make_float4(v.x, v.y, v.z, V4.w);
+            const bool is_bead = id < P.nb;
+            const float4 V = vel_of(id);
+            float3 v = scaled(V);
+            if (!is_bead || P.srd_rotate_beads) {
+                const float3 d = v - u;
+                const float rx = d.x * ca - d.y * sa;
+                const float ry = d.x * sa + d.y * ca;
+                v = make_float3(u.x + rx, u.y + ry, u.z + d.z);
+                if (scale2) v = make_float3(u.x + lam2 * (v.x - u.x), u.y + lam2 * (v.y - u.y), v.z);
+            }
+            if (is_bead) {
+                if (lab || P.srd_rotate_beads) bvel[id] = make_float4(v.x, v.y, v.z, V.w);
+            } else {
+                const float4 P4 = sp_old[id - P.nb];
+                float3 p = f3(P4);
+                const float3 dr = dt_srd * v;
+                p += dr;
+                apply_boundaries(P, p, v, dr, 0.0f);
+                const uint32_t dst = s0 + (k - nbc);
+                sp_new[dst] = make_float4(p.x, p.y, p.z, P4.w);
+                sv_new[dst] = make_float4(v.x, v.y, v.z, V.w);
+            }
         }
     }
     S.srd_mean[c] = make_float4(u.x, u.y, u.z, 0.f);
 }
+
+// The collision just written the solvent to the other buffer.
+__global__ void srd_flip_kernel(uint32_t* scur) { *scur ^= 1u; }
 
 __global__ void advance_step_kernel(unsigned long long* step_base, unsigned long long k) { *step_base += k; }
 

@@ -33,16 +33,22 @@ struct StepBuffers {
     // in-place views of the sorted path (= pos2[0], ...)
     float4 *pos, *vel, *force, *force_old, *tangent;
     uint32_t *hash, *slot, *tmp_index, *sorted_index, *sorted_hash;
-    // solvent state (particle nb + k is solvent k)
-    float4 *spos, *svel;
+    // solvent state (particle nb + k is solvent k), kept in the cell order of
+    // the last collision: each collision reads [*scur] and writes [*scur ^ 1]
+    float4 *spos2[2], *svel2[2];
+    uint32_t* scur;
     // capped per-cell bead lists of the cell-list path: counts of update n in
     // lcount[n % 3], members in lslot[n & 1][cell * cap + slot]
     uint32_t *lcount[3], *lslot[2];
     uint32_t cap;
     uint32_t *cell_count, *cell_offset, *cell_start, *cell_end, *chunk_count;
     float4 *sorted_pos, *sorted_vel, *sorted_tan;
-    uint32_t *srd_hash, *srd_slot, *srd_tmp, *srd_sorted_index;
-    uint32_t *srd_count, *srd_offset, *srd_start, *srd_end, *srd_chunk;
+    // SRD collision: per-particle cell hash and slot (beads [0, nb), solvent
+    // [nb, ntotal)); beads and solvent are bucketed separately (a cell's
+    // members in the stable order are its beads, then its solvent)
+    uint32_t *srd_hash, *srd_slot, *srd_btmp, *srd_stmp, *srd_sorted_index;
+    uint32_t *srd_bcount, *srd_scount, *srd_boff, *srd_soff, *srd_bchunk, *srd_schunk;
+    uint32_t *srd_start, *srd_end;
     float4* srd_mean;
     uint32_t* err;
     unsigned long long* step_base;
@@ -397,6 +403,9 @@ __global__ void __launch_bounds__(256) srd_hash_kernel(const DevParams P, const 
 // solvent's ballistic streaming by dt_srd (solvent_integrator, :145-205).
 __global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
                                                           float dt_srd, uint32_t buf_sel);
+
+__global__ void __launch_bounds__(256) srd_scatter_kernel(const DevParams P, const StepBuffers S);
+__global__ void srd_flip_kernel(uint32_t* scur);
 
 __global__ void advance_step_kernel(unsigned long long* step_base, unsigned long long k);
 

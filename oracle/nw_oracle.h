@@ -96,7 +96,10 @@ uint32_t nwo_num_srd_cells(const NwConfig* cfg);
                       uint64_t step, R dt, uint32_t* hash_out, uint32_t* sorted_index_out,        \
                       uint32_t* cell_start_out, uint32_t* cell_end_out);                          \
     /* SRD grid shift of a collision at `step` (world units). */                                  \
-    void nwo_srd_shift_##S(const NwConfig* cfg, uint64_t step, float shift[3]);
+    void nwo_srd_shift_##S(const NwConfig* cfg, uint64_t step, float shift[3]);                   \
+    /* Relabel the solvent in the collision's stable cell order (the engine's storage order). */  \
+    void nwo_reorder_solvent_##S(R* pos, R* vel, uint32_t n_beads, uint32_t n_solvent,            \
+                                 const uint32_t* sorted_index);
 
 NWO_DECLARE(float, f32)
 NWO_DECLARE(double, f64)

@@ -699,6 +699,33 @@ void RS(nwo_step)(const NwConfig* cfg, R* pos, R* vel, R* force, R* force_old, R
     if (cfg->srd_enabled && cfg->srd_gap > 0 && (step % cfg->srd_gap) == 0) {
         float shift[3];
         RS(nwo_srd_shift)(cfg, step, shift);
-        RS(nwo_srd)(cfg, pos, vel, nb, ns, shift, NULL, step, dt * (R)cfg->srd_gap, NULL, NULL, NULL, NULL);
+        uint32_t* order = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)(nb + ns ? nb + ns : 1));
+        RS(nwo_srd)(cfg, pos, vel, nb, ns, shift, NULL, step, dt * (R)cfg->srd_gap, order, NULL, NULL, NULL);
+        RS(nwo_reorder_solvent)(pos, vel, nb, ns, order);
+        free(order);
     }
+}
+
+/* The engine stores the solvent in the cell order of the last collision:
+ * solvent particle k after a collision is the k-th solvent entry of the
+ * collision's stable (cell, index) order.  Solvent particles are identical,
+ * so this relabelling changes no physics. */
+void RS(nwo_reorder_solvent)(R* pos, R* vel, uint32_t n_beads, uint32_t n_solvent, const uint32_t* sorted_index)
+{
+    R* np_ = (R*)malloc(sizeof(R) * 4 * (size_t)(n_solvent ? n_solvent : 1));
+    R* nv_ = (R*)malloc(sizeof(R) * 4 * (size_t)(n_solvent ? n_solvent : 1));
+    size_t k = 0;
+    for (size_t q = 0; q < (size_t)n_beads + n_solvent; ++q) {
+        const uint32_t id = sorted_index[q];
+        if (id < n_beads) continue;
+        for (int c = 0; c < 4; ++c) {
+            np_[4 * k + c] = pos[4 * (size_t)id + c];
+            nv_[4 * k + c] = vel[4 * (size_t)id + c];
+        }
+        ++k;
+    }
+    memcpy(pos + 4 * (size_t)n_beads, np_, sizeof(R) * 4 * (size_t)n_solvent);
+    memcpy(vel + 4 * (size_t)n_beads, nv_, sizeof(R) * 4 * (size_t)n_solvent);
+    free(np_);
+    free(nv_);
 }

@@ -66,6 +66,7 @@ def lib() -> C.CDLL:
             getattr(L, f"nwo_srd_{s}").argtypes = [_CP, _P, _P, _u32, _u32, _P, _P, _u64, R, _P, _P, _P, _P]
             getattr(L, f"nwo_step_{s}").argtypes = [_CP, _P, _P, _P, _P, _P, _u64, R, _P, _P, _P, _P]
             getattr(L, f"nwo_srd_shift_{s}").argtypes = [_CP, _u64, _P]
+            getattr(L, f"nwo_reorder_solvent_{s}").argtypes = [_P, _P, _u32, _u32, _P]
         _lib = L
     return _lib
 
@@ -219,6 +220,16 @@ def srd(cfg, pos, vel, n_beads, n_solvent, shift, rot_uniform=None, step=0, dt_s
     getattr(lib(), f"nwo_srd_{s}")(C.byref(cfg), _ptr(p), _ptr(v), n_beads, n_solvent, _ptr(sh), _ptr(ru), step,
                                    dt_srd, _ptr(si), _ptr(cs), _ptr(ce), _ptr(cm))
     return dict(pos=p, vel=v, sorted_index=si, cell_start=cs, cell_end=ce, cell_mean=cm)
+
+
+def reorder_solvent(pos, vel, n_beads, n_solvent, sorted_index, prec=32):
+    """Solvent relabelled in the collision's stable cell order (the order the
+    engine stores it in after a collision); beads unchanged."""
+    dt_, s = _dt(prec)
+    p, v = _f4(pos, dt_), _f4(vel, dt_)
+    si = np.ascontiguousarray(np.asarray(sorted_index, dtype=np.uint32))
+    getattr(lib(), f"nwo_reorder_solvent_{s}")(_ptr(p), _ptr(v), n_beads, n_solvent, _ptr(si))
+    return p, v
 
 
 def srd_shift(cfg, step, prec=32):

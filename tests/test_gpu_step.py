@@ -90,7 +90,7 @@ def run_oracle(orc, cfg, pos, vel, tan, nsteps=1, prec=32):
 CASES = ["wca", "wca_srd", "wca_reverse", "ref", "ref_srd", "ref_walls"]
 STRATEGIES = [abi.NW_STRATEGY_CELL_LISTS, abi.NW_STRATEGY_SORTED]
 # launches of one update: (bead step, SRD collision) + the step counter
-LAUNCHES = {abi.NW_STRATEGY_CELL_LISTS: (2, 5), abi.NW_STRATEGY_SORTED: (6, 5)}
+LAUNCHES = {abi.NW_STRATEGY_CELL_LISTS: (2, 8), abi.NW_STRATEGY_SORTED: (6, 8)}
 
 
 @pytest.mark.parametrize("strategy", STRATEGIES)
