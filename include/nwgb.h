@@ -278,6 +278,14 @@ typedef struct NwKernelTime {
 } NwKernelTime;
 nw_status nw_profile_steps(nw_system* sys, int nsteps, float dt, NwKernelTime* out, int max_entries, int* n_entries);
 
+/* Numerics self-check of the refined reciprocal, square root and quotient
+ * the force laws use (no reference counterpart).  For host arrays a[n] and
+ * b[n] of positive normal floats it writes, per element, out[4*i + 0..3] =
+ * 1/a, sqrt(a), a/b computed by the device helpers, and the hardware
+ * reciprocal square root of a.  Allocates and frees its own device buffers;
+ * synchronous. */
+nw_status nw_math_probe(const float* a, const float* b, uint32_t n, float* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -42,7 +42,26 @@ struct DevParams {
     float srd_alpha, srd_kT, srd_shift_lo;
     int32_t srd_rotate_beads, srd_thermo;
     uint32_t seed_lo, seed_hi;
+    // multiply-shift divisors by grid[0] and grid[0] * grid[1] (see fast_div)
+    uint32_t div_gx_m, div_gx_k, div_gxy_m, div_gxy_k;
 };
+
+// floor(n / d) for n < 2^30 and 1 <= d < 2^30 with m = floor(2^k / d) + 1,
+// k = 30 + ceil(log2 d): n * m / 2^k = n / d + e with 0 < e < 1 / d
+// (Granlund and Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994).
+__host__ __device__ __forceinline__ uint32_t fast_div(uint32_t n, uint32_t m, uint32_t k)
+{
+    return (uint32_t)(((unsigned long long)n * m) >> k);
+}
+
+inline void fast_div_params(uint32_t d, uint32_t& m, uint32_t& k)
+{
+    uint32_t l = 0;
+    while ((1ull << l) < (unsigned long long)d) ++l;
+    k = 30u + l;
+    m = (uint32_t)((1ull << k) / d + 1ull);
+}
 
 // ---- float3 helpers --------------------------------------------------------
 __device__ __forceinline__ float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }
@@ -148,7 +167,8 @@ __device__ __forceinline__ int3 grid_pos(const DevParams& P, float3 p)
     int3 g;
     g.x = (int)floorf((p.x - P.origin[0]) / P.cell[0]);
     g.y = (int)floorf((p.y - P.origin[1]) / P.cell[1]);
-    g.z = (int)floorf((p.z - P.origin[2]) / P.cell[2]);
+    // a single layer maps every z to cell 0 in all hash modes
+    g.z = P.grid[2] == 1u ? 0 : (int)floorf((p.z - P.origin[2]) / P.cell[2]);
     return g;
 }
 
@@ -197,8 +217,8 @@ __device__ __forceinline__ uint32_t srd_hash(const DevParams& P, float3 p, float
             if (rel >= P.box[a]) rel -= P.box[a];
             else if (rel < 0.0f) rel += P.box[a];
         }
-        const int g = (int)floorf(rel / P.srd_cell[a]);
         const uint32_t G = P.srd_grid[a];
+        const int g = G == 1u ? 0 : (int)floorf(rel / P.srd_cell[a]);
         if (P.bnd[a] == NW_PERIODIC)
             c[a] = P.hash_mode == NW_HASH_MASK ? ((uint32_t)g & (G - 1u)) : wrap_mod(g, G);
         else

@@ -64,6 +64,8 @@ DevParams make_dev_params(const NwConfig& c, float dt)
     P.srd_thermo = c.srd_thermostat;
     P.seed_lo = (uint32_t)c.seed;
     P.seed_hi = (uint32_t)(c.seed >> 32);
+    fast_div_params(P.grid[0] ? P.grid[0] : 1u, P.div_gx_m, P.div_gx_k);
+    fast_div_params(P.grid[0] * P.grid[1] ? P.grid[0] * P.grid[1] : 1u, P.div_gxy_m, P.div_gxy_k);
     return P;
 }
 

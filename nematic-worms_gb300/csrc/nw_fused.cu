@@ -79,40 +79,29 @@ __device__ __forceinline__ int cell_members(const uint32_t* __restrict__ cnt, co
 template <int CAP>
 __device__ __forceinline__ float3 wca_list_force(const DevParams& P, const float4* __restrict__ pos,
                                                  const uint32_t* __restrict__ cnt,
-                                                 const uint32_t* __restrict__ slots, uint32_t i, float3 r)
+                                                 const uint32_t* __restrict__ slots, uint32_t i, float3 r,
+                                                 uint32_t own)
 {
-    const int3 g = grid_pos(P, r);
-    uint32_t cx[3], cy[3], cz[3];
-    const int nx = axis_cells(P, 0, cell_coord(P, 0, g.x), cx);
-    const int ny = axis_cells(P, 1, cell_coord(P, 1, g.y), cy);
-    const int nz = axis_cells(P, 2, cell_coord(P, 2, g.z), cz);
-    const uint32_t fI = i / P.L;
+    const uint32_t fbase = (i / P.L) * P.L;
     float3 f = zero3();
-    for (int kz = 0; kz < nz; ++kz)
-        for (int ky = 0; ky < ny; ++ky)
-            for (int kx = 0; kx < nx; ++kx) {
-                const uint32_t h = (cz[kz] * P.grid[1] + cy[ky]) * P.grid[0] + cx[kx];
-                uint32_t ids[CAP];
-                const int k = cell_members<CAP>(cnt, slots, h, ids);
+    for_neighbour_cells(P, r, own, [&](uint32_t h) {
+        uint32_t ids[CAP];
+        const int k = cell_members<CAP>(cnt, slots, h, ids);
 #pragma unroll
-                for (int m = 0; m < CAP; ++m) {
-                    if (m >= k) break;
-                    const uint32_t j = ids[m];
-                    if (j == i) continue;
-                    const int d = (int)j - (int)i;
-                    if (d <= P.lj_exclude && d >= -P.lj_exclude && j / P.L == fI) continue;
-                    float3 dr = f3(__ldg(pos + j)) - r;
-                    min_image(P, dr);
-                    const float rr = dot3(dr, dr);
-                    if (rr > P.lj_rc2) continue;
-                    const float rr4 = rr * rr * rr * rr;
-                    const float rr7 = rr * rr * rr * rr * rr * rr * rr;
-                    const float fm = P.lj_amp * ((P.lj_two_s6 / rr7) - (1.0f / rr4));
-                    f.x -= fm * dr.x;
-                    f.y -= fm * dr.y;
-                    f.z -= fm * dr.z;
-                }
-            }
+        for (int m = 0; m < CAP; ++m) {
+            if (m >= k) break;
+            const uint32_t j = ids[m];
+            if (j == i || lj_excluded(P, i, j, fbase)) continue;
+            float3 dr = f3(__ldg(pos + j)) - r;
+            min_image(P, dr);
+            const float rr = dot3(dr, dr);
+            if (rr > P.lj_rc2) continue;
+            const float fm = wca_lj(P, rr);
+            f.x -= fm * dr.x;
+            f.y -= fm * dr.y;
+            f.z -= fm * dr.z;
+        }
+    });
     return f;
 }
 
@@ -213,7 +202,7 @@ __device__ __forceinline__ float3 list_pair_force(const DevParams& P, const Step
     const uint32_t* slots = S.lslot[cur];
     const float3 r = f3(S.pos2[cur][i]);
     if (kRef) return ref_list_force<CAP>(P, S.pos2[cur], S.vel2[cur], S.tan2[cur], cnt, slots, i, r);
-    return wca_list_force<CAP>(P, S.pos2[cur], cnt, slots, i, r);
+    return wca_list_force<CAP>(P, S.pos2[cur], cnt, slots, i, r, S.hash2[cur][i]);
 }
 
 // Shared-memory bytes of the pro part for a block of `beads` beads.
@@ -326,9 +315,8 @@ __device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& 
     }
     if (P.model == NW_MODEL_WCA_WORMS) {
         const float3 me = f3(R[c]);
-        if (c + 1 < L) wca_bond(P, me, f3(R[c + 1]), fs);
         if (c > 0) wca_bond(P, me, f3(R[c - 1]), fs);
-        if (c + 1 < L) wca_drive(P, me, f3(R[c + 1]), fs);
+        if (c + 1 < L) wca_bond_drive(P, me, f3(R[c + 1]), fs);
     }
     S.pos2[out][i] = nP;
     S.vel2[out][i] = nV;

@@ -90,9 +90,8 @@ __global__ void __launch_bounds__(1024) filament_pass_kernel(const DevParams P, 
     }
     if (P.model == NW_MODEL_WCA_WORMS) {
         const float3 me = f3(R[c]);
-        if (c + 1 < L) wca_bond(P, me, f3(R[c + 1]), fs);
         if (c > 0) wca_bond(P, me, f3(R[c - 1]), fs);
-        if (c + 1 < L) wca_drive(P, me, f3(R[c + 1]), fs);
+        if (c + 1 < L) wca_bond_drive(P, me, f3(R[c + 1]), fs);
     }
     S.pos[i] = nP;
     S.vel[i] = nV;
@@ -191,45 +190,30 @@ __global__ void __launch_bounds__(256) pair_wca_kernel(const DevParams P, const 
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P.nb) return;
     const float3 r = f3(S.sorted_pos[p]);
-    const int3 g = grid_pos(P, r);
-    uint32_t cx[3], cy[3], cz[3];
-    const int nx = axis_cells(P, 0, cell_coord(P, 0, g.x), cx);
-    const int ny = axis_cells(P, 1, cell_coord(P, 1, g.y), cy);
-    const int nz = axis_cells(P, 2, cell_coord(P, 2, g.z), cz);
     const uint32_t me = S.sorted_index[p];
     if (me >= P.nb) {
         atomicOr(S.err, (uint32_t)NW_EFLAG_BAD_INDEX);
         return;
     }
-    const uint32_t fI = me / P.L;
-    const int cI = (int)(me - fI * P.L);
+    const uint32_t fbase = (me / P.L) * P.L;
     float3 f = zero3();
-    for (int kz = 0; kz < nz; ++kz)
-        for (int ky = 0; ky < ny; ++ky)
-            for (int kx = 0; kx < nx; ++kx) {
-                const uint32_t h = (cz[kz] * P.grid[1] + cy[ky]) * P.grid[0] + cx[kx];
-                uint32_t s0, s1;
-                if (!cell_range(P, S, h, s0, s1)) continue;
-                for (uint32_t j = s0; j < s1; ++j) {
-                    if (j == p) continue;
-                    const uint32_t o = __ldg(&S.sorted_index[j]);
-                    const uint32_t fJ = o / P.L;
-                    if (fJ == fI) {
-                        const int d = (int)(o - fJ * P.L) - cI;
-                        if (d <= P.lj_exclude && d >= -P.lj_exclude) continue;
-                    }
-                    float3 dr = f3(__ldg(&S.sorted_pos[j])) - r;
-                    min_image(P, dr);
-                    const float rr = dot3(dr, dr);
-                    if (rr > P.lj_rc2) continue;
-                    const float rr4 = rr * rr * rr * rr;
-                    const float rr7 = rr * rr * rr * rr * rr * rr * rr;
-                    const float fm = P.lj_amp * ((P.lj_two_s6 / rr7) - (1.0f / rr4));
-                    f.x -= fm * dr.x;
-                    f.y -= fm * dr.y;
-                    f.z -= fm * dr.z;
-                }
-            }
+    for_neighbour_cells(P, r, S.sorted_hash[p], [&](uint32_t h) {
+        uint32_t s0, s1;
+        if (!cell_range(P, S, h, s0, s1)) return;
+        for (uint32_t j = s0; j < s1; ++j) {
+            if (j == p) continue;
+            const uint32_t o = __ldg(&S.sorted_index[j]);
+            if (lj_excluded(P, me, o, fbase)) continue;
+            float3 dr = f3(__ldg(&S.sorted_pos[j])) - r;
+            min_image(P, dr);
+            const float rr = dot3(dr, dr);
+            if (rr > P.lj_rc2) continue;
+            const float fm = wca_lj(P, rr);
+            f.x -= fm * dr.x;
+            f.y -= fm * dr.y;
+            f.z -= fm * dr.z;
+        }
+    });
     float4 F = S.force[me];
     F.x += f.x;
     F.y += f.y;
@@ -420,3 +404,41 @@ __global__ void srd_flip_kernel(uint32_t* scur) { *scur ^= 1u; }
 __global__ void advance_step_kernel(unsigned long long* step_base, unsigned long long k) { *step_base += k; }
 
 }  // namespace nw
+
+namespace {
+
+__global__ void math_probe_kernel(const float* a, const float* b, uint32_t n, float4* out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float x = a[i], y = b[i];
+    const float r = rsqrtf(x);
+    out[i] = make_float4(nw::rcp_nr(x), nw::sqrt_nr(x, r), nw::div_nr(x, y), r);
+}
+
+}  // namespace
+
+extern "C" nw_status nw_math_probe(const float* a, const float* b, uint32_t n, float* out)
+{
+    if (!a || !b || !out) return NW_ERR_INVALID;
+    if (n == 0) return NW_OK;
+    float *da = nullptr, *db = nullptr, *dout = nullptr;
+    cudaError_t e = cudaMalloc(&da, (size_t)n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&db, (size_t)n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&dout, (size_t)n * 16);
+    if (e == cudaSuccess) e = cudaMemcpy(da, a, (size_t)n * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(db, b, (size_t)n * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        math_probe_kernel<<<(n + 255) / 256, 256>>>(da, db, n, reinterpret_cast<float4*>(dout));
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, (size_t)n * 16, cudaMemcpyDeviceToHost);
+    cudaFree(da);
+    cudaFree(db);
+    cudaFree(dout);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return NW_ERR_CUDA;
+    }
+    return NW_OK;
+}

@@ -81,19 +81,54 @@ __device__ __forceinline__ uint32_t count_into_cell(uint32_t* cell_count, uint32
 
 // ---- bonded helpers ----------------------------------------------------------
 
-// One bending triple (filamentKernel, particles_kernel_impl.cuh:777-800).
 struct Triple {
     float3 fi, fj, fk;
 };
+// The bonded and pair laws below avoid IEEE division and square-root
+// sequences (with their slow-path calls): they start from the hardware
+// approximations (__fdividef, rsqrtf; <= 2 ulp) and, where the reference's
+// result involves cancellation (r - r0 of a bond, the bending projections,
+// the two LJ terms), refine them by one Newton-Raphson step whose residual
+// is formed exactly with an FMA (P. Markstein, "Computation of elementary
+// functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34,
+// 1990).  Inputs are finite, positive and normal (squared separations of
+// distinct beads).  nw_math_probe exposes the three for tests.
+
+// 1/x to about 1 ulp: y' = y + y (1 - x y).
+__device__ __forceinline__ float rcp_nr(float x)
+{
+    const float y = __fdividef(1.0f, x);
+    return fmaf(y, fmaf(-x, y, 1.0f), y);
+}
+
+// sqrt(q) to about 1 ulp from y ~ 1/sqrt(q): r = q y, r' = r + (y / 2) (q - r^2).
+__device__ __forceinline__ float sqrt_nr(float q, float y)
+{
+    const float r = q * y;
+    return fmaf(0.5f * y, fmaf(-r, r, q), r);
+}
+
+// a / b to about 1 ulp: t = a (1/b), t' = t + (1/b) (a - b t).
+__device__ __forceinline__ float div_nr(float a, float b)
+{
+    const float y = rcp_nr(b);
+    const float t = a * y;
+    return fmaf(fmaf(-b, t, a), y, t);
+}
+
+// One bending triple (filamentKernel, particles_kernel_impl.cuh:777-800):
+// A = k_b / (d_ij d_jk), F_i = -A (r_jk - r_ij (r_ij . r_jk) / d_ij^2),
+// F_k = -A (r_jk (r_ij . r_jk) / d_jk^2 - r_ij), F_j = -F_i - F_k.
 __device__ __forceinline__ Triple bend_triple(const DevParams& P, float3 ri, float3 rj, float3 rk)
 {
     float3 rij = rj - ri, rjk = rk - rj;
-    const float dij = min_image_len(P, rij);
-    const float djk = min_image_len(P, rjk);
+    min_image(P, rij);
+    min_image(P, rjk);
+    const float qij = dot3(rij, rij), qjk = dot3(rjk, rjk);
     const float dd = dot3(rij, rjk);
-    const float A = P.bend_k / (dij * djk);
-    const float3 B = (rij * dd) / dot3(rij, rij);
-    const float3 C = (rjk * dd) / dot3(rjk, rjk);
+    const float A = P.bend_k * (rsqrtf(qij) * rsqrtf(qjk));
+    const float3 B = rij * div_nr(dd, qij);
+    const float3 C = rjk * div_nr(dd, qjk);
     Triple t;
     t.fi = (-A) * (rjk - B);
     t.fk = (-A) * (C - rij);
@@ -101,35 +136,71 @@ __device__ __forceinline__ Triple bend_triple(const DevParams& P, float3 ri, flo
     return t;
 }
 
-// getTangent (particles_kernel_impl.cuh:303-309).
+// getTangent (particles_kernel_impl.cuh:303-309): the unit vector a -> b.
 __device__ __forceinline__ float3 tangent_of(const DevParams& P, float3 a, float3 b)
 {
     float3 rel = b - a;
-    const float d = min_image_len(P, rel);
-    return rel / d;
+    min_image(P, rel);
+    return rel * rsqrtf(dot3(rel, rel));
 }
 
-// Archived harmonic bond (NWWormsKernel_InternalForce.h:37-59).
+// Archived harmonic bond (NWWormsKernel_InternalForce.h:37-59):
+// F_i = k (|r| - r0) r / |r| with r = r_j - r_i.
 __device__ __forceinline__ void wca_bond(const DevParams& P, float3 ri, float3 rj, float3& f)
 {
     float3 dr = rj - ri;
     min_image(P, dr);
-    const float r = sqrtf(dot3(dr, dr));
-    const float fm = -(P.bond_k * (r - P.bond_r0)) / r;
+    const float q = dot3(dr, dr);
+    const float ir = rsqrtf(q);
+    const float fm = -(P.bond_k * (sqrt_nr(q, ir) - P.bond_r0)) * ir;
     f.x -= fm * dr.x;
     f.y -= fm * dr.y;
     f.z -= fm * dr.z;
 }
 
-// Archived tangent drive (NWWormsKernel_DriveForce.h:21-34).
+// Archived tangent drive (NWWormsKernel_DriveForce.h:21-34): F_act along
+// the unit vector to the next bead.
 __device__ __forceinline__ void wca_drive(const DevParams& P, float3 ri, float3 rn, float3& f)
 {
     float3 dr = rn - ri;
     min_image(P, dr);
-    const float m = sqrtf(dot3(dr, dr));
-    f.x += P.activity * (dr.x / m);
-    f.y += P.activity * (dr.y / m);
-    f.z += P.activity * (dr.z / m);
+    const float s = P.activity * rsqrtf(dot3(dr, dr));
+    f.x += s * dr.x;
+    f.y += s * dr.y;
+    f.z += s * dr.z;
+}
+
+// The bond to the next bead and the drive along it share one separation
+// and one reciprocal square root.
+__device__ __forceinline__ void wca_bond_drive(const DevParams& P, float3 ri, float3 rn, float3& f)
+{
+    float3 dr = rn - ri;
+    min_image(P, dr);
+    const float q = dot3(dr, dr);
+    const float ir = rsqrtf(q);
+    const float fm = -(P.bond_k * (sqrt_nr(q, ir) - P.bond_r0)) * ir;
+    const float s = P.activity * ir;
+    f.x += s * dr.x - fm * dr.x;
+    f.y += s * dr.y - fm * dr.y;
+    f.z += s * dr.z - fm * dr.z;
+}
+
+// Repulsive LJ magnitude of NWWormsKernel_LennardJones.h:38-50,
+// 24 eps s^6 (2 s^6 / r^14 - 1 / r^8), from one reciprocal of r^2.
+__device__ __forceinline__ float wca_lj(const DevParams& P, float rr)
+{
+    const float ir = rcp_nr(rr);
+    const float ir2 = ir * ir;
+    const float ir4 = ir2 * ir2;
+    return P.lj_amp * (P.lj_two_s6 * (ir4 * ir2 * ir) - ir4);
+}
+
+// Same-filament pairs closer than lj_exclude along the chain take no LJ
+// force; fbase = first bead of bead i's filament.
+__device__ __forceinline__ bool lj_excluded(const DevParams& P, uint32_t i, uint32_t j, uint32_t fbase)
+{
+    const int d = (int)j - (int)i;
+    return d <= P.lj_exclude && d >= -P.lj_exclude && j - fbase < P.L;
 }
 
 // ---- K1: filament pass ---------------------------------------------------------
@@ -352,26 +423,80 @@ __device__ __forceinline__ float3 ref_cell_sum(const DevParams& P, const StepBuf
 // z, y, x order, which reproduces the reference's accumulation exactly.
 __global__ void __launch_bounds__(256) pair_ref_kernel(const DevParams P, const StepBuffers S);
 
-// Distinct neighbour cells of one axis under modulo wrap (or clipping at walls),
-// in increasing offset order.
-__device__ __forceinline__ int axis_cells(const DevParams& P, int a, uint32_t c, uint32_t out[3])
+// Neighbour cell c + o (o in -1..1) of one axis as the distinct-cell visit
+// takes it: wrapped on periodic axes, absent beyond a wall, and absent when
+// an earlier offset already gave the same cell (possible only with fewer
+// than three cells on the axis).
+__device__ __forceinline__ bool nb_cell(const DevParams& P, int a, uint32_t c, int o, uint32_t& out)
 {
     const int G = (int)P.grid[a];
-    int n = 0;
-#pragma unroll
-    for (int o = -1; o <= 1; ++o) {
-        int x = (int)c + o;
-        if (P.bnd[a] == NW_PERIODIC) {
+    const bool per = P.bnd[a] == NW_PERIODIC;
+    auto at = [&](int oo, int& x) -> bool {
+        x = (int)c + oo;
+        if (per) {
             if (x < 0) x += G;
             else if (x >= G) x -= G;
-        } else if (x < 0 || x >= G) {
-            continue;
+            return true;
         }
-        bool dup = false;
-        for (int k = 0; k < n; ++k) dup |= out[k] == (uint32_t)x;
-        if (!dup) out[n++] = (uint32_t)x;
+        return x >= 0 && x < G;
+    };
+    int x;
+    if (!at(o, x)) return false;
+    if (G < 3) {
+        for (int q = -1; q < o; ++q) {
+            int y;
+            if (at(q, y) && y == x) return false;
+        }
     }
-    return n;
+    out = (uint32_t)x;
+    return true;
+}
+
+// Cell coordinates of a modulo/clamp cell hash h = (cz * Gy + cy) * Gx + cx,
+// by multiply-shift division.
+__device__ __forceinline__ void cell_of_hash(const DevParams& P, uint32_t h, uint32_t& cx, uint32_t& cy, uint32_t& cz)
+{
+    uint32_t rest = h;
+    cz = 0;
+    if (P.grid[2] > 1u) {
+        cz = fast_div(h, P.div_gxy_m, P.div_gxy_k);
+        rest = h - cz * (P.grid[0] * P.grid[1]);
+    }
+    cy = fast_div(rest, P.div_gx_m, P.div_gx_k);
+    cx = rest - cy * P.grid[0];
+}
+
+// visit(h) for every distinct neighbour cell h of a bead at r whose own
+// cell hash is `own`, in the reference's z, y, x order.
+template <class Visit>
+__device__ __forceinline__ void for_neighbour_cells(const DevParams& P, float3 r, uint32_t own, Visit visit)
+{
+    uint32_t c0, c1, c2;
+    if (P.hash_mode == NW_HASH_MASK) {
+        const int3 g = grid_pos(P, r);
+        c0 = cell_coord(P, 0, g.x);
+        c1 = cell_coord(P, 1, g.y);
+        c2 = cell_coord(P, 2, g.z);
+    } else {
+        cell_of_hash(P, own, c0, c1, c2);
+    }
+#pragma unroll 1
+    for (int dz = -1; dz <= 1; ++dz) {
+        uint32_t z;
+        if (!nb_cell(P, 2, c2, dz, z)) continue;
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; ++dy) {
+            uint32_t y;
+            if (!nb_cell(P, 1, c1, dy, y)) continue;
+            const uint32_t row = (z * P.grid[1] + y) * P.grid[0];
+#pragma unroll 1
+            for (int dx = -1; dx <= 1; ++dx) {
+                uint32_t x;
+                if (!nb_cell(P, 0, c0, dx, x)) continue;
+                visit(row + x);
+            }
+        }
+    }
 }
 
 // WCA_WORMS pair pass: repulsive LJ to every bead within lj_rcut in the

@@ -196,6 +196,7 @@ HANDLE_API = [
     ("nw_config_size", C.c_size_t, []),
     ("nw_last_launch_count", C.c_int, [_sysp, C.POINTER(C.c_uint64)]),
     ("nw_profile_steps", C.c_int, [_sysp, C.c_int, _f32, C.POINTER(NwKernelTime), C.c_int, C.POINTER(C.c_int)]),
+    ("nw_math_probe", C.c_int, [C.c_void_p, C.c_void_p, _u32, C.c_void_p]),
 ]
 
 _fp = C.c_void_p  # device pointers are passed as integers
