@@ -42,14 +42,14 @@
 extern "C" {
 #endif
 
-#define NW_ABI_VERSION 1u
+#define NW_ABI_VERSION 2u
 
 typedef int nw_status;
 enum {
     NW_OK = 0,
     NW_ERR_CUDA = 1,          /* a CUDA runtime call failed */
     NW_ERR_INVALID = 2,       /* bad argument or configuration */
-    NW_ERR_CELL_OVERFLOW = 3, /* a cell held more particles than a kernel's capacity */
+    NW_ERR_CELL_OVERFLOW = 3, /* a cell or neighbour list held more particles than its capacity */
     NW_ERR_NONFINITE = 4,     /* a non-finite position or force was produced */
     NW_ERR_TIMEOUT = 5,       /* a bounded device wait gave up */
     NW_ERR_NOMEM = 6,         /* device or host allocation failed */
@@ -62,7 +62,8 @@ enum {
     NW_EFLAG_NONFINITE = 1u << 0,
     NW_EFLAG_CELL_OVERFLOW = 1u << 1,
     NW_EFLAG_TIMEOUT = 1u << 2,
-    NW_EFLAG_BAD_INDEX = 1u << 3
+    NW_EFLAG_BAD_INDEX = 1u << 3,
+    NW_EFLAG_NEIGHBOR_OVERFLOW = 1u << 4
 };
 
 typedef enum { NW_MODEL_WCA_WORMS = 0, NW_MODEL_REF_DEM = 1 } nw_model;
@@ -141,8 +142,10 @@ typedef struct NwConfig {
     uint64_t seed;
     float    dt;
     int32_t  strategy;         /* nw_strategy: how a step finds its neighbours */
-    uint32_t cell_capacity;    /* beads a cell list holds (NW_STRATEGY_CELL_LISTS): 8 or 16; 0 = by model */
-    uint32_t reserved[5];
+    uint32_t cell_capacity;    /* beads a cell list holds (CELL_LISTS, VERLET): 8 or 16; 0 = by model */
+    float    neighbor_skin;    /* VERLET: list radius = lj_rcut + skin; 0 = 0.3 lj_sigma */
+    uint32_t neighbor_capacity;/* VERLET: neighbours a bead's list holds; 0 = 32 */
+    uint32_t reserved[3];
 } NwConfig;
 
 /* Neighbour search of the bead step.
@@ -154,8 +157,21 @@ typedef struct NwConfig {
  *              sorted order and cell bounds are produced only when read.
  *              A cell with more beads than cell_capacity is reported as
  *              NW_ERR_CELL_OVERFLOW.
- *  AUTO        CELL_LISTS. */
-typedef enum { NW_STRATEGY_AUTO = 0, NW_STRATEGY_SORTED = 1, NW_STRATEGY_CELL_LISTS = 2 } nw_strategy;
+ *  VERLET      (WCA_WORMS) CELL_LISTS on cells of at least lj_rcut + skin,
+ *              from which each bead keeps the list of beads within that
+ *              radius; steps reuse the lists while the summed maximum bead
+ *              displacement since they were built stays below skin / 2, so
+ *              every pair within lj_rcut is on them, and rebuild them in the
+ *              pair pass otherwise.  Same forces as CELL_LISTS up to the
+ *              order of the FP32 sums.
+ *  AUTO        VERLET for WCA_WORMS, CELL_LISTS for REF_DEM (whose pair set
+ *              is all beads of the neighbour cells, not a radius). */
+typedef enum {
+    NW_STRATEGY_AUTO = 0,
+    NW_STRATEGY_SORTED = 1,
+    NW_STRATEGY_CELL_LISTS = 2,
+    NW_STRATEGY_VERLET = 3
+} nw_strategy;
 
 /* Array selectors for nw_get_array / nw_set_array / nw_device_array. */
 typedef enum {

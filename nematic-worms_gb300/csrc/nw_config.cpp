@@ -149,8 +149,11 @@ nw_status nw_config_validate(const NwConfig* c)
             if (c->grid[a] > 1 && c->cell_size[a] < c->lj_rcut * (1.0f - 1e-6f)) return NW_ERR_INVALID;
     }
     if (!std::isfinite(c->dt)) return NW_ERR_INVALID;
-    if (c->strategy < NW_STRATEGY_AUTO || c->strategy > NW_STRATEGY_CELL_LISTS) return NW_ERR_INVALID;
+    if (c->strategy < NW_STRATEGY_AUTO || c->strategy > NW_STRATEGY_VERLET) return NW_ERR_INVALID;
+    if (c->strategy == NW_STRATEGY_VERLET && c->model != NW_MODEL_WCA_WORMS) return NW_ERR_INVALID;
     if (c->cell_capacity != 0 && c->cell_capacity != 8 && c->cell_capacity != 16) return NW_ERR_INVALID;
+    if (!std::isfinite(c->neighbor_skin) || c->neighbor_skin < 0.0f) return NW_ERR_INVALID;
+    if (c->neighbor_capacity != 0 && (c->neighbor_capacity < 4 || c->neighbor_capacity > 256)) return NW_ERR_INVALID;
     if (c->srd_enabled) {
         uint64_t nsc = 1;
         for (int a = 0; a < 3; ++a) {

@@ -44,6 +44,17 @@ struct DevParams {
     uint32_t seed_lo, seed_hi;
     // multiply-shift divisors by grid[0] and grid[0] * grid[1] (see fast_div)
     uint32_t div_gx_m, div_gx_k, div_gxy_m, div_gxy_k;
+    // float reciprocals of the bead and SRD cell sizes (see floor_div)
+    float inv_cell[3], srd_inv_cell[3];
+    // cell grid of the per-step bead lists: the reference grid, or with
+    // Verlet lists (vl_on) cells of at least lj_rcut + skin on the same box
+    int32_t vl_on;
+    uint32_t lgrid[3], lncells;
+    float linv[3];  // lgrid / box
+    uint32_t ldiv_x_m, ldiv_x_k, ldiv_xy_m, ldiv_xy_k;
+    float vl_r2;         // (lj_rcut + skin)^2
+    float vl_half_skin;  // lists stay valid while the displacement bound is below this
+    uint32_t vl_cap;     // neighbours per bead list
 };
 
 // floor(n / d) for n < 2^30 and 1 <= d < 2^30 with m = floor(2^k / d) + 1,
@@ -107,6 +118,15 @@ __host__ __device__ __forceinline__ uint4 rng_draw(const DevParams& P, uint32_t 
 __host__ __device__ __forceinline__ float u01(uint32_t x) { return ((float)(x >> 9) + 0.5f) * 1.1920928955078125e-07f; }
 
 // Two Box-Muller pairs: four standard normals.
+// The first Box-Muller pair of normal4 only (2D systems use two components).
+__device__ __forceinline__ float2 normal2(uint4 x)
+{
+    float s0, c0;
+    const float r0 = sqrtf(-2.0f * logf(u01(x.x)));
+    sincospif(2.0f * u01(x.y), &s0, &c0);
+    return make_float2(r0 * c0, r0 * s0);
+}
+
 __device__ __forceinline__ float4 normal4(uint4 x)
 {
     float s0, c0, s1, c1;
@@ -115,6 +135,18 @@ __device__ __forceinline__ float4 normal4(uint4 x)
     sincospif(2.0f * u01(x.y), &s0, &c0);
     sincospif(2.0f * u01(x.w), &s1, &c1);
     return make_float4(r0 * c0, r0 * s0, r1 * c1, r1 * s1);
+}
+
+// Langevin noise sigma * (z0, z1[, z2]) of one Philox draw; 2D systems need
+// only the first Box-Muller pair.
+__device__ __forceinline__ float3 noise3(const DevParams& P, uint4 x)
+{
+    if (P.dim >= 3) {
+        const float4 z = normal4(x);
+        return make_float3(P.noise_sigma * z.x, P.noise_sigma * z.y, P.noise_sigma * z.z);
+    }
+    const float2 z = normal2(x);
+    return make_float3(P.noise_sigma * z.x, P.noise_sigma * z.y, 0.f);
 }
 
 // ---- geometry ----------------------------------------------------------------
@@ -160,22 +192,43 @@ __device__ __forceinline__ void min_image(const DevParams& P, float3& d)
     }
 }
 
-// calcGridPos (particles_kernel_impl.cuh:231-238): IEEE division, floor,
-// saturating float->int.
+// floor(x / c) as the reference computes it (IEEE quotient, floor,
+// saturating float -> int), for c > 0 with ic = 1/c rounded to float.
+// x * ic and the IEEE quotient both lie within 1.2e-7 |q| of the exact x / c,
+// so their floors agree unless an integer lies within that distance; only
+// then is the division itself evaluated.
+__device__ __forceinline__ int floor_div(float x, float c, float ic)
+{
+    const float q = x * ic;
+    const float n = rintf(q);
+    if (fabsf(q - n) <= fabsf(q) * 5.0e-7f) return (int)floorf(x / c);
+    return (int)floorf(q);
+}
+
+// calcGridPos (particles_kernel_impl.cuh:231-238).
 __device__ __forceinline__ int3 grid_pos(const DevParams& P, float3 p)
 {
     int3 g;
-    g.x = (int)floorf((p.x - P.origin[0]) / P.cell[0]);
-    g.y = (int)floorf((p.y - P.origin[1]) / P.cell[1]);
+    g.x = floor_div(p.x - P.origin[0], P.cell[0], P.inv_cell[0]);
+    g.y = floor_div(p.y - P.origin[1], P.cell[1], P.inv_cell[1]);
     // a single layer maps every z to cell 0 in all hash modes
-    g.z = P.grid[2] == 1u ? 0 : (int)floorf((p.z - P.origin[2]) / P.cell[2]);
+    g.z = P.grid[2] == 1u ? 0 : floor_div(p.z - P.origin[2], P.cell[2], P.inv_cell[2]);
     return g;
 }
 
+// g mod G in [0, G): one compare for the cells inside the box and one add or
+// subtract for a single wrap; the integer remainder only beyond that.
 __device__ __forceinline__ uint32_t wrap_mod(int g, uint32_t G)
 {
-    int m = g % (int)G;
-    return (uint32_t)(m < 0 ? m + (int)G : m);
+    const int n = (int)G;
+    if (g >= 0) {
+        if (g < n) return (uint32_t)g;
+        if (g - n < n) return (uint32_t)(g - n);
+    } else if (g >= -n) {
+        return (uint32_t)(g + n);
+    }
+    const int m = g % n;
+    return (uint32_t)(m < 0 ? m + n : m);
 }
 
 __device__ __forceinline__ uint32_t clamp_cell(int g, uint32_t G)
@@ -204,6 +257,21 @@ __device__ __forceinline__ uint32_t bead_hash(const DevParams& P, float3 p)
     return cell_hash(P, cell_coord(P, 0, g.x), cell_coord(P, 1, g.y), cell_coord(P, 2, g.z));
 }
 
+// Cell of a bead on the Verlet list grid (modulo hash, no exactness
+// requirement: insertion and lookup use this one function).
+__device__ __forceinline__ uint32_t list_hash(const DevParams& P, float3 p)
+{
+    const float x[3] = {p.x, p.y, p.z};
+    uint32_t c[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const uint32_t G = P.lgrid[a];
+        const int g = G == 1u ? 0 : (int)floorf((x[a] - P.origin[a]) * P.linv[a]);
+        c[a] = P.bnd[a] == NW_PERIODIC ? wrap_mod(g, G) : clamp_cell(g, G);
+    }
+    return (c[2] * P.lgrid[1] + c[1]) * P.lgrid[0] + c[0];
+}
+
 // positionRelativeToBox + calcGridPosSRD + calcGridHashSRD
 // (particles_kernel_impl.cuh:208-228, 241-249, 261-276); wall axes clamped.
 __device__ __forceinline__ uint32_t srd_hash(const DevParams& P, float3 p, float3 shift)
@@ -218,7 +286,7 @@ __device__ __forceinline__ uint32_t srd_hash(const DevParams& P, float3 p, float
             else if (rel < 0.0f) rel += P.box[a];
         }
         const uint32_t G = P.srd_grid[a];
-        const int g = G == 1u ? 0 : (int)floorf(rel / P.srd_cell[a]);
+        const int g = G == 1u ? 0 : floor_div(rel, P.srd_cell[a], P.srd_inv_cell[a]);
         if (P.bnd[a] == NW_PERIODIC)
             c[a] = P.hash_mode == NW_HASH_MASK ? ((uint32_t)g & (G - 1u)) : wrap_mod(g, G);
         else

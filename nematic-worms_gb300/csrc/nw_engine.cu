@@ -32,6 +32,8 @@ DevParams make_dev_params(const NwConfig& c, float dt)
         P.bnd[a] = c.boundary[a];
         P.srd_grid[a] = c.srd_grid[a] ? c.srd_grid[a] : 1u;
         P.srd_cell[a] = c.srd_cell_size[a];
+        P.inv_cell[a] = 1.0f / c.cell_size[a];
+        P.srd_inv_cell[a] = c.srd_cell_size[a] > 0.0f ? 1.0f / c.srd_cell_size[a] : 0.0f;
     }
     P.srd_ncells = P.srd_grid[0] * P.srd_grid[1] * P.srd_grid[2];
     P.radius = c.radius;
@@ -66,6 +68,32 @@ DevParams make_dev_params(const NwConfig& c, float dt)
     P.seed_hi = (uint32_t)(c.seed >> 32);
     fast_div_params(P.grid[0] ? P.grid[0] : 1u, P.div_gx_m, P.div_gx_k);
     fast_div_params(P.grid[0] * P.grid[1] ? P.grid[0] * P.grid[1] : 1u, P.div_gxy_m, P.div_gxy_k);
+    // per-step bead lists: the reference grid, or the Verlet list grid
+    P.vl_on = effective_strategy(c) == NW_STRATEGY_VERLET && c.model == NW_MODEL_WCA_WORMS;
+    const float skin = c.neighbor_skin > 0.0f ? c.neighbor_skin : 0.3f * c.lj_sigma;
+    const float rl = c.lj_rcut + skin;
+    P.vl_r2 = rl * rl;
+    P.vl_half_skin = 0.5f * skin;
+    P.vl_cap = c.neighbor_capacity ? c.neighbor_capacity : 32u;
+    P.lncells = 1;
+    for (int a = 0; a < 3; ++a) {
+        if (P.vl_on) {
+            // cells a little wider than the list radius, tiling the box exactly
+            uint32_t G = 1;
+            if (c.grid[a] > 1u) {
+                const float g = std::floor(c.box[a] / (rl * 1.0001f));
+                G = g >= 1.0f ? (uint32_t)g : 1u;
+            }
+            P.lgrid[a] = G;
+            P.linv[a] = (float)G / c.box[a];
+        } else {
+            P.lgrid[a] = P.grid[a];
+            P.linv[a] = P.inv_cell[a];
+        }
+        P.lncells *= P.lgrid[a];
+    }
+    fast_div_params(P.lgrid[0], P.ldiv_x_m, P.ldiv_x_k);
+    fast_div_params(P.lgrid[0] * P.lgrid[1], P.ldiv_xy_m, P.ldiv_xy_k);
     return P;
 }
 
@@ -161,6 +189,15 @@ __global__ void __launch_bounds__(256) count_hash_kernel(const uint32_t* __restr
     if (i < n) slot[i] = count_into_cell(count, hash[i]);
 }
 
+// Reference-grid cell hash of every bead (systems whose per-step lists live
+// on the Verlet grid compute it only when it is read).
+__global__ void __launch_bounds__(256) ref_hash_kernel(const DevParams P, const float4* __restrict__ pos,
+                                                       uint32_t* __restrict__ hash)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P.nb) hash[i] = bead_hash(P, f3(pos[i]));
+}
+
 }  // namespace nw
 
 using namespace nw;
@@ -182,12 +219,16 @@ struct nw_system {
     StepBuffers B;
     bool lists = false;  // NW_STRATEGY_CELL_LISTS
     uint32_t nb = 0, ns = 0, ntotal = 0, ncells = 0, nchunks = 0, srd_ncells = 0, srd_nchunks = 0;
+    uint32_t lncells = 0;  // cells of the per-step bead lists (>= the reference grid's when Verlet cells are finer)
     uint64_t step = 0;
     uint64_t version = 1;
     bool use_graphs = true;
     bool lists_dirty = false;  // list counters must be cleared before the next update
     uint64_t sorted_for = ~0ull;  // step whose sorted order / cell bounds are in the sort buffers
     uint32_t scur = 0;            // solvent buffer holding the current solvent (mirror of *B.scur)
+    bool vl = false;              // NW_STRATEGY_VERLET: hash2 holds Verlet-grid hashes
+    bool vl_dirty = true;         // Verlet lists must be rebuilt at the next update
+    uint64_t hash_for = ~0ull;    // step whose reference hashes are in hash2[cur] (Verlet systems)
     std::vector<GraphEntry> graphs;
     uint64_t last_launches = 0;
     std::vector<void*> allocs;
@@ -257,10 +298,17 @@ uint32_t collision_parity(const nw_system* s, uint64_t first, int nsteps)
 // Clear the list counters when the step counter changed under them.
 cudaError_t clean_lists(nw_system* s)
 {
+    if (s->vl && s->vl_dirty) {
+        // an unbounded displacement forces a list build at the next pair pass
+        const uint32_t init[8] = {0x7f000000u, 0x7f000000u, 0u, 0u, 0u, 0u, 0u, 0u};
+        cudaError_t e = cudaMemcpyAsync(s->B.vstate, init, sizeof(init), cudaMemcpyHostToDevice, s->stream);
+        if (e != cudaSuccess) return e;
+        s->vl_dirty = false;
+    }
     if (!s->lists || !s->lists_dirty) return cudaSuccess;
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < 3 && e == cudaSuccess; ++k)
-        e = cudaMemsetAsync(s->B.lcount[k], 0, ((size_t)s->ncells + 8) * 4, s->stream);
+        e = cudaMemsetAsync(s->B.lcount[k], 0, ((size_t)s->lncells + 8) * 4, s->stream);
     if (e == cudaSuccess) s->lists_dirty = false;
     return e;
 }
@@ -309,9 +357,22 @@ uint64_t enqueue_steps(nw_system* s, int nsteps, float dt, uint64_t first_step, 
 
 // Sorted order and cell bounds of the current bead hashes (cell-list systems
 // keep no sorted order between updates; this runs the counting sort once).
+cudaError_t ensure_hash(nw_system* s)
+{
+    if (!s->vl || s->hash_for == s->step || s->nb == 0) return cudaSuccess;
+    const DevParams P = make_dev_params(s->cfg, s->cfg.dt);
+    const uint32_t cur = cur_buffer(s);
+    ref_hash_kernel<<<cdiv(s->nb, 256), 256, 0, s->stream>>>(P, s->B.pos2[cur], s->B.hash2[cur]);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) s->hash_for = s->step;
+    return e;
+}
+
 cudaError_t ensure_sorted(nw_system* s)
 {
     if (!s->lists || s->sorted_for == s->step || s->nb == 0) return cudaSuccess;
+    cudaError_t eh = ensure_hash(s);
+    if (eh != cudaSuccess) return eh;
     const DevParams P = make_dev_params(s->cfg, s->cfg.dt);
     StepBuffers B = s->B;
     const uint32_t cur = cur_buffer(s);
@@ -346,7 +407,15 @@ nw_status transfer(nw_system* s, int array, void* host, uint32_t start, uint32_t
     case NW_TANGENT: bead_ptr = B.tan2[cur]; break;
     case NW_FORCE: bead_ptr = B.force; break;
     case NW_FORCE_OLD: bead_ptr = B.force_old; break;
-    case NW_HASH: bead_ptr = B.hash2[cur]; elem = 4; break;
+    case NW_HASH: {
+        if (dir == Dir::ToHost) {
+            cudaError_t e = ensure_hash(s);
+            if (e != cudaSuccess) return cuda_status(e);
+        }
+        bead_ptr = B.hash2[cur];
+        elem = 4;
+        break;
+    }
     case NW_SORTED_INDEX:
     case NW_CELL_START:
     case NW_CELL_END: {
@@ -389,7 +458,11 @@ nw_status transfer(nw_system* s, int array, void* host, uint32_t start, uint32_t
                                  : cudaMemcpyAsync(h, d, (b - a) * elem, cudaMemcpyDeviceToHost, s->stream);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    if (dir == Dir::ToDevice) s->sorted_for = ~0ull;
+    if (dir == Dir::ToDevice) {
+        s->sorted_for = ~0ull;
+        s->hash_for = ~0ull;
+        if (array == NW_POSITION) s->vl_dirty = true;
+    }
     return cuda_status(e);
 }
 
@@ -416,11 +489,19 @@ nw_status nw_create(const NwConfig* cfg, nw_system** out)
         return NW_ERR_CUDA;
     }
     s->stream = s->own_stream;
-    s->lists = cfg->strategy != NW_STRATEGY_SORTED;
+    s->lists = effective_strategy(*cfg) != NW_STRATEGY_SORTED;
+    const DevParams P0 = make_dev_params(*cfg, cfg->dt);
+    s->vl = P0.vl_on != 0;
+    if (P0.lncells >= (1u << 30)) {
+        cudaStreamDestroy(s->own_stream);
+        delete s;
+        return NW_ERR_INVALID;
+    }
     s->nb = cfg->num_filaments * cfg->filament_size;
     s->ns = cfg->srd_enabled ? cfg->num_solvent : 0u;
     s->ntotal = s->nb + s->ns;
     s->ncells = cfg->grid[0] * cfg->grid[1] * cfg->grid[2];
+    s->lncells = P0.lncells > s->ncells ? P0.lncells : s->ncells;
     s->nchunks = (s->ncells + kChunk - 1) / kChunk;
     s->srd_ncells = cfg->srd_enabled ? cfg->srd_grid[0] * cfg->srd_grid[1] * cfg->srd_grid[2] : 0u;
     s->srd_nchunks = (s->srd_ncells + kChunk - 1) / kChunk;
@@ -472,8 +553,14 @@ nw_status nw_create(const NwConfig* cfg, nw_system** out)
         A(alloc_n(s, &B.sorted_tan, nb));
     }
     if (s->lists) {
-        for (int k = 0; k < 3; ++k) A(alloc_n(s, &B.lcount[k], C + 8));
-        for (int k = 0; k < 2; ++k) A(alloc_n(s, &B.lslot[k], C * B.cap + 8));
+        const size_t LC = P0.lncells > C ? P0.lncells : C;
+        for (int k = 0; k < 3; ++k) A(alloc_n(s, &B.lcount[k], LC + 8));
+        for (int k = 0; k < 2; ++k) A(alloc_n(s, &B.lslot[k], LC * B.cap + 8));
+    }
+    if (s->vl) {
+        A(alloc_n(s, &B.nbr, (size_t)P0.vl_cap * nb + 8));
+        A(alloc_n(s, &B.nnb, nb + 8));
+        A(alloc_n(s, &B.vstate, 8));
     }
     if (cfg->srd_enabled) {
         const size_t Cs = s->srd_ncells, nt = s->ntotal;
@@ -522,7 +609,7 @@ nw_status nw_create(const NwConfig* cfg, nw_system** out)
     Z(B.cell_start, (C + 8) * 4, 0xff);
     Z(B.cell_end, (C + 8) * 4, 0xff);
     if (s->lists)
-        for (int k = 0; k < 3; ++k) Z(B.lcount[k], (C + 8) * 4);
+        for (int k = 0; k < 3; ++k) Z(B.lcount[k], ((size_t)s->lncells + 8) * 4);
     if (cfg->srd_enabled) {
         Z(B.srd_bcount, ((size_t)s->srd_ncells + 8) * 4);
         Z(B.srd_scount, ((size_t)s->srd_ncells + 8) * 4);
@@ -563,7 +650,16 @@ nw_status nw_set_config(nw_system* s, const NwConfig* cfg)
     for (int a = 0; a < 3; ++a)
         if (cfg->grid[a] != o.grid[a] || (cfg->srd_enabled && cfg->srd_grid[a] != o.srd_grid[a]))
             return NW_ERR_INVALID;
+    // the list buffers were sized for the old list grid and list capacity
+    const DevParams Pn = make_dev_params(*cfg, cfg->dt), Po = make_dev_params(o, o.dt);
+    if (Pn.vl_on != Po.vl_on || Pn.lncells != Po.lncells || (Pn.vl_on && Pn.vl_cap != Po.vl_cap))
+        return NW_ERR_INVALID;
+    for (int a = 0; a < 3; ++a)
+        if (Pn.lgrid[a] != Po.lgrid[a]) return NW_ERR_INVALID;
     s->cfg = *cfg;
+    s->vl_dirty = true;  // radii or the box may have changed
+    s->hash_for = ~0ull;
+    s->sorted_for = ~0ull;
     drop_graphs(s);
     return NW_OK;
 }
@@ -604,12 +700,23 @@ nw_status nw_device_array(nw_system* s, int array, void** dptr)
     const StepBuffers& B = s->B;
     void* p = nullptr;
     switch (array) {
-    case NW_POSITION: p = B.pos2[cur]; break;
+    case NW_POSITION:
+        p = B.pos2[cur];
+        s->vl_dirty = true;  // the caller may move beads through the pointer
+        s->hash_for = ~0ull;
+        s->sorted_for = ~0ull;
+        break;
     case NW_VELOCITY: p = B.vel2[cur]; break;
     case NW_TANGENT: p = B.tan2[cur]; break;
     case NW_FORCE: p = B.force; break;
     case NW_FORCE_OLD: p = B.force_old; break;
-    case NW_HASH: p = B.hash2[cur]; break;
+    case NW_HASH: {
+        cudaError_t e = ensure_hash(s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) return cuda_status(e);
+        p = B.hash2[cur];
+        break;
+    }
     case NW_SORTED_INDEX:
     case NW_CELL_START:
     case NW_CELL_END: {
@@ -700,7 +807,7 @@ nw_status nw_sync(nw_system* s)
     nw_status st = nw_error_word(s, &f);
     if (st != NW_OK) return st;
     if (f & NW_EFLAG_NONFINITE) return NW_ERR_NONFINITE;
-    if (f & NW_EFLAG_CELL_OVERFLOW) return NW_ERR_CELL_OVERFLOW;
+    if (f & (NW_EFLAG_CELL_OVERFLOW | NW_EFLAG_NEIGHBOR_OVERFLOW)) return NW_ERR_CELL_OVERFLOW;
     if (f & NW_EFLAG_TIMEOUT) return NW_ERR_TIMEOUT;
     if (f & NW_EFLAG_BAD_INDEX) return NW_ERR_INVALID;
     return NW_OK;
@@ -735,7 +842,9 @@ nw_status nw_set_step(nw_system* s, uint64_t step)
     if (e == cudaSuccess) {
         s->step = step;
         s->lists_dirty = true;
+        s->vl_dirty = true;
         s->sorted_for = ~0ull;
+        s->hash_for = ~0ull;
     }
     return cuda_status(e);
 }

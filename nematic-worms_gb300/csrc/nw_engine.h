@@ -21,6 +21,13 @@ struct Prof {
     void clear();
 };
 
+// The neighbour search a configuration runs (NW_STRATEGY_AUTO resolved).
+inline int effective_strategy(const NwConfig& c)
+{
+    if (c.strategy != NW_STRATEGY_AUTO) return c.strategy;
+    return c.model == NW_MODEL_WCA_WORMS ? NW_STRATEGY_VERLET : NW_STRATEGY_CELL_LISTS;
+}
+
 // Kernel parameter block for a configuration and step size.
 DevParams make_dev_params(const NwConfig& c, float dt);
 

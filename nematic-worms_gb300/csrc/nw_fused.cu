@@ -84,7 +84,7 @@ __device__ __forceinline__ float3 wca_list_force(const DevParams& P, const float
 {
     const uint32_t fbase = (i / P.L) * P.L;
     float3 f = zero3();
-    for_neighbour_cells(P, r, own, [&](uint32_t h) {
+    for_neighbour_cells<true>(P, r, own, [&](uint32_t h) {
         uint32_t ids[CAP];
         const int k = cell_members<CAP>(cnt, slots, h, ids);
 #pragma unroll
@@ -192,6 +192,88 @@ __device__ __forceinline__ float3 ref_list_force(const DevParams& P, const float
     return total;
 }
 
+// Displacement bound of the state after update n: the bound after update
+// n - 1 (zero if the lists were built then) plus update n's largest bead
+// displacement.  Every block reads the same words, so all agree.
+__device__ __forceinline__ float vl_bound(const StepBuffers& S, unsigned long long n)
+{
+    return __uint_as_float(S.vstate[(uint32_t)((n + 1ull) & 1ull)]) +
+           __uint_as_float(S.vstate[2u + (uint32_t)(n % 3ull)]);
+}
+
+// Verlet pair force: the bead's list from the last build, each pair still
+// tested against lj_rcut.  Pairs are summed in list order, which is the
+// cell-scan order of the build.
+__device__ __forceinline__ float3 verlet_force(const DevParams& P, const StepBuffers& S,
+                                               const float4* __restrict__ pos, uint32_t i, float3 r)
+{
+    uint32_t k = __ldg(S.nnb + i);
+    if (k > P.vl_cap) k = P.vl_cap;
+    float3 f = zero3();
+    const uint32_t* __restrict__ col = S.nbr + i;
+    for (uint32_t m = 0; m < k; ++m) {
+        const uint32_t j = __ldg(col + (size_t)m * P.nb);
+        float3 dr = f3(__ldg(pos + j)) - r;
+        min_image(P, dr);
+        const float rr = dot3(dr, dr);
+        if (rr > P.lj_rc2) continue;
+        const float fm = wca_lj(P, rr);
+        f.x -= fm * dr.x;
+        f.y -= fm * dr.y;
+        f.z -= fm * dr.z;
+    }
+    return f;
+}
+
+// List build: the cell scan of wca_list_force on the Verlet grid, recording
+// every non-excluded bead within lj_rcut + skin and summing the LJ force of
+// those within lj_rcut.
+template <int CAP>
+__device__ __forceinline__ float3 verlet_build_force(const DevParams& P, const StepBuffers& S,
+                                                     const float4* __restrict__ pos,
+                                                     const uint32_t* __restrict__ cnt,
+                                                     const uint32_t* __restrict__ slots, uint32_t i, float3 r,
+                                                     uint32_t own)
+{
+    const uint32_t fbase = (i / P.L) * P.L;
+    uint32_t k = 0;
+    uint32_t* col = S.nbr + i;
+    float3 f = zero3();
+    for_neighbour_cells<true>(P, r, own, [&](uint32_t h) {
+        uint32_t ids[CAP];
+        const int kc = cell_members<CAP>(cnt, slots, h, ids);
+#pragma unroll
+        for (int m = 0; m < CAP; ++m) {
+            if (m >= kc) break;
+            const uint32_t j = ids[m];
+            if (j == i || lj_excluded(P, i, j, fbase)) continue;
+            float3 dr = f3(__ldg(pos + j)) - r;
+            min_image(P, dr);
+            const float rr = dot3(dr, dr);
+            if (rr > P.vl_r2) continue;
+            if (k < P.vl_cap) col[(size_t)k * P.nb] = j;
+            ++k;
+            if (rr > P.lj_rc2) continue;
+            const float fm = wca_lj(P, rr);
+            f.x -= fm * dr.x;
+            f.y -= fm * dr.y;
+            f.z -= fm * dr.z;
+        }
+    });
+    S.nnb[i] = k < P.vl_cap ? k : P.vl_cap;
+    if (k > P.vl_cap) atomicOr(S.err, (uint32_t)NW_EFLAG_NEIGHBOR_OVERFLOW);
+    return f;
+}
+
+// Bookkeeping of the Verlet lists by the kernel that runs the pair pass of
+// update n (one thread): the bound after update n, and a cleared maximum for
+// update n + 2.
+__device__ __forceinline__ void vl_commit(const StepBuffers& S, unsigned long long n, bool rebuilt, float bound)
+{
+    S.vstate[(uint32_t)(n & 1ull)] = __float_as_uint(rebuilt ? 0.0f : bound);
+    S.vstate[2u + (uint32_t)((n + 2ull) % 3ull)] = 0u;
+}
+
 // Pair force of bead i for update n (reads the update-n buffers and list).
 template <int CAP, bool kRef>
 __device__ __forceinline__ float3 list_pair_force(const DevParams& P, const StepBuffers& S, unsigned long long n,
@@ -202,6 +284,13 @@ __device__ __forceinline__ float3 list_pair_force(const DevParams& P, const Step
     const uint32_t* slots = S.lslot[cur];
     const float3 r = f3(S.pos2[cur][i]);
     if (kRef) return ref_list_force<CAP>(P, S.pos2[cur], S.vel2[cur], S.tan2[cur], cnt, slots, i, r);
+    if (P.vl_on) {
+        const float bound = vl_bound(S, n);
+        const bool rebuild = !(bound <= P.vl_half_skin);  // a NaN bound rebuilds too
+        if (blockIdx.x == 0 && threadIdx.x == 0) vl_commit(S, n, rebuild, bound);
+        if (!rebuild) return verlet_force(P, S, S.pos2[cur], i, r);
+        return verlet_build_force<CAP>(P, S, S.pos2[cur], cnt, slots, i, r, S.hash2[cur][i]);
+    }
     return wca_list_force<CAP>(P, S.pos2[cur], cnt, slots, i, r, S.hash2[cur][i]);
 }
 
@@ -230,10 +319,11 @@ __device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& 
     {
         uint32_t* nxt = S.lcount[(uint32_t)((n + 1ull) % 3ull)];
         const uint32_t stride = gridDim.x * blockDim.x;
-        for (uint32_t c = blockIdx.x * blockDim.x + t; c < P.ncells; c += stride) nxt[c] = 0u;
+        for (uint32_t c = blockIdx.x * blockDim.x + t; c < P.lncells; c += stride) nxt[c] = 0u;
     }
 
     float4 nP = make_float4(0.f, 0.f, 0.f, 0.f), nV = nP, nFo = nP;
+    float disp2 = 0.f;  // squared displacement of this update (Verlet list bound)
     if (active) {
         const float4 P4 = S.pos2[in][i], V4 = S.vel2[in][i], Fo4 = S.force_old[i];
         float3 p = f3(P4), v = f3(V4);
@@ -243,6 +333,7 @@ __device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& 
         v += dv;
         const float3 dr = v * dt + ((0.5f * f) * dt) * dt;
         p += dr;
+        disp2 = dot3(dr, dr);
         apply_boundaries(P, p, v, dr, P.radius);
         nP = make_float4(p.x, p.y, p.z, P4.w);
         nV = make_float4(v.x, v.y, v.z, V4.w);
@@ -261,12 +352,18 @@ __device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& 
             const float u = u01(rng_draw(P, w0 + wl, n, kRngReverse).x);
             if (u <= P.reverse_p) {
                 const uint32_t src = wl * L + (L - 1u - c);
+                disp2 = 3.0e38f;  // bead indices moved: the lists must be rebuilt
                 nP = smp[src];
                 nV = smp[beads + src];
                 nFo = smp[2 * beads + src];
             }
         }
         __syncthreads();
+    }
+    if (P.vl_on) {
+        // largest displacement of update n (float bits order like the values)
+        const uint32_t m = __reduce_max_sync(0xffffffffu, __float_as_uint(disp2));
+        if ((t & 31u) == 0u && m) atomicMax(&S.vstate[2u + (uint32_t)(n % 3ull)], __float_as_uint(sqrtf(__uint_as_float(m))));
     }
     if (active) smp[t] = nP;
     __syncthreads();
@@ -285,8 +382,7 @@ __device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& 
     float3 fs = zero3();
     if (P.langevin_on) {
         // langevinKernel (particles_kernel_impl.cuh:859-874), Philox noise in registers
-        const float4 z = normal4(rng_draw(P, i, n, kRngLangevin));
-        const float3 g = make_float3(P.noise_sigma * z.x, P.noise_sigma * z.y, P.dim >= 3 ? P.noise_sigma * z.z : 0.f);
+        const float3 g = noise3(P, rng_draw(P, i, n, kRngLangevin));
         float3 fl = zero3() - P.gamma * f3(nV);
         fl += g;
         fs = fl;
@@ -325,7 +421,7 @@ __device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& 
     S.tan2[out][i] = wt ? make_float4(tg.x, tg.y, tg.z, 0.f) : S.tan2[in][i];
     if (!finite3(f3(nP)) || !finite3(fs)) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
 
-    const uint32_t h = bead_hash(P, f3(nP));
+    const uint32_t h = P.vl_on ? list_hash(P, f3(nP)) : bead_hash(P, f3(nP));
     S.hash2[out][i] = h;
     const uint32_t slot = atomicAdd(&S.lcount[(uint32_t)(n % 3ull)][h], 1u);
     if (slot < (uint32_t)CAP) S.lslot[out][(size_t)h * CAP + slot] = i;

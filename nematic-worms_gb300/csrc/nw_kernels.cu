@@ -60,8 +60,7 @@ __global__ void __launch_bounds__(1024) filament_pass_kernel(const DevParams P, 
     float3 fs = zero3();
     if (P.langevin_on) {
         // langevinKernel (particles_kernel_impl.cuh:859-874), Philox noise in registers
-        const float4 z = normal4(rng_draw(P, i, step, kRngLangevin));
-        const float3 g = make_float3(P.noise_sigma * z.x, P.noise_sigma * z.y, P.dim >= 3 ? P.noise_sigma * z.z : 0.f);
+        const float3 g = noise3(P, rng_draw(P, i, step, kRngLangevin));
         float3 fl = zero3() - P.gamma * f3(nV);
         fl += g;
         fs = fl;
@@ -197,7 +196,7 @@ __global__ void __launch_bounds__(256) pair_wca_kernel(const DevParams P, const 
     }
     const uint32_t fbase = (me / P.L) * P.L;
     float3 f = zero3();
-    for_neighbour_cells(P, r, S.sorted_hash[p], [&](uint32_t h) {
+    for_neighbour_cells<false>(P, r, S.sorted_hash[p], [&](uint32_t h) {
         uint32_t s0, s1;
         if (!cell_range(P, S, h, s0, s1)) return;
         for (uint32_t j = s0; j < s1; ++j) {
@@ -224,17 +223,27 @@ __global__ void __launch_bounds__(256) pair_wca_kernel(const DevParams P, const 
 
 // SRD cell hash of every particle (beads from the current bead buffer,
 // solvent from the current solvent buffer) and its slot in its cell's bead
-// or solvent bucket.  Lanes of a warp that share a bucket take consecutive
-// slots from one atomic (the solvent is stored in cell order, so a warp's
-// particles fall into few cells).
+// or solvent bucket.  The solvent is stored in cell order, so equal keys come
+// in runs along the warp: the first lane of each run takes the run's slots
+// with one atomic.  The grid shift of a scheduled collision is drawn once per
+// block.
 __global__ void __launch_bounds__(256) srd_hash_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
                                                        int shift_from_step, float3 shift, uint32_t buf_sel)
 {
-    // every lane of the warp takes part in the match (blockDim is a multiple of 32)
+    __shared__ float s_shift[3];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < P.ntotal;
     const unsigned long long step = *S.step_base + step_off;
-    if (shift_from_step) shift = srd_shift_of(P, step);
+    if (shift_from_step) {
+        if (threadIdx.x == 0) {
+            const float3 d = srd_shift_of(P, step);
+            s_shift[0] = d.x;
+            s_shift[1] = d.y;
+            s_shift[2] = d.z;
+        }
+        __syncthreads();
+        shift = make_float3(s_shift[0], s_shift[1], s_shift[2]);
+    }
     const uint32_t cur = buf_sel < 2u ? buf_sel : (uint32_t)(step & 1ull);
     const bool bead = i < P.nb;
     uint32_t h = 0, key = 0xffffffffu;  // no cell hash reaches 2^31 - 1 with the bead bit set
@@ -244,13 +253,18 @@ __global__ void __launch_bounds__(256) srd_hash_kernel(const DevParams P, const 
         S.srd_hash[i] = h;
         key = h | (bead ? 0x80000000u : 0u);
     }
-    const uint32_t peers = __match_any_sync(0xffffffffu, key);
-    const int lane = (int)(threadIdx.x & 31u);
-    const int leader = __ffs(peers) - 1;
+    // every lane of the warp takes part (blockDim is a multiple of 32)
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
+    const uint32_t heads = __ballot_sync(0xffffffffu, lane == 0u || prev != key);
+    const uint32_t upto = (2u << lane) - 1u;  // lanes 0..lane (all 32 bits for lane 31)
+    const uint32_t start = 31u - (uint32_t)__clz(heads & upto);
+    const uint32_t after = heads & ~upto;
+    const uint32_t end = after ? (uint32_t)(__ffs(after) - 1) : 32u;
     uint32_t base = 0;
-    if (valid && lane == leader) base = atomicAdd(bead ? &S.srd_bcount[h] : &S.srd_scount[h], (uint32_t)__popc(peers));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (valid) S.srd_slot[i] = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+    if (valid && lane == start) base = atomicAdd(bead ? &S.srd_bcount[h] : &S.srd_scount[h], end - start);
+    base = __shfl_sync(0xffffffffu, base, (int)start);
+    if (valid) S.srd_slot[i] = base + (lane - start);
 }
 
 // Bucket every particle: beads by bead index, solvent by solvent index.

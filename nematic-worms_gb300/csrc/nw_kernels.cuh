@@ -41,6 +41,11 @@ struct StepBuffers {
     // lcount[n % 3], members in lslot[n & 1][cell * cap + slot]
     uint32_t *lcount[3], *lslot[2];
     uint32_t cap;
+    // Verlet lists (vl_on): neighbours of bead i in nbr[k * nb + i], k < nnb[i];
+    // vstate[0..1] displacement bound of the state after update n in [n & 1],
+    // vstate[2..4] maximum bead displacement of update n in [2 + n % 3]
+    // (float bits; the bound counts from the last list build)
+    uint32_t *nbr, *nnb, *vstate;
     uint32_t *cell_count, *cell_offset, *cell_start, *cell_end, *chunk_count;
     float4 *sorted_pos, *sorted_vel, *sorted_tan;
     // SRD collision: per-particle cell hash and slot (beads [0, nb), solvent
@@ -423,14 +428,12 @@ __device__ __forceinline__ float3 ref_cell_sum(const DevParams& P, const StepBuf
 // z, y, x order, which reproduces the reference's accumulation exactly.
 __global__ void __launch_bounds__(256) pair_ref_kernel(const DevParams P, const StepBuffers S);
 
-// Neighbour cell c + o (o in -1..1) of one axis as the distinct-cell visit
-// takes it: wrapped on periodic axes, absent beyond a wall, and absent when
-// an earlier offset already gave the same cell (possible only with fewer
-// than three cells on the axis).
-__device__ __forceinline__ bool nb_cell(const DevParams& P, int a, uint32_t c, int o, uint32_t& out)
+// Neighbour cell c + o (o in -1..1) of an axis of G cells as the
+// distinct-cell visit takes it: wrapped on periodic axes, absent beyond a
+// wall, and absent when an earlier offset already gave the same cell
+// (possible only with fewer than three cells on the axis).
+__device__ __forceinline__ bool nb_cell(int G, bool per, uint32_t c, int o, uint32_t& out)
 {
-    const int G = (int)P.grid[a];
-    const bool per = P.bnd[a] == NW_PERIODIC;
     auto at = [&](int oo, int& x) -> bool {
         x = (int)c + oo;
         if (per) {
@@ -452,47 +455,46 @@ __device__ __forceinline__ bool nb_cell(const DevParams& P, int a, uint32_t c, i
     return true;
 }
 
-// Cell coordinates of a modulo/clamp cell hash h = (cz * Gy + cy) * Gx + cx,
-// by multiply-shift division.
-__device__ __forceinline__ void cell_of_hash(const DevParams& P, uint32_t h, uint32_t& cx, uint32_t& cy, uint32_t& cz)
-{
-    uint32_t rest = h;
-    cz = 0;
-    if (P.grid[2] > 1u) {
-        cz = fast_div(h, P.div_gxy_m, P.div_gxy_k);
-        rest = h - cz * (P.grid[0] * P.grid[1]);
-    }
-    cy = fast_div(rest, P.div_gx_m, P.div_gx_k);
-    cx = rest - cy * P.grid[0];
-}
-
 // visit(h) for every distinct neighbour cell h of a bead at r whose own
-// cell hash is `own`, in the reference's z, y, x order.
-template <class Visit>
+// cell hash is `own`, in the reference's z, y, x order.  kList selects the
+// per-step list grid (the Verlet grid when vl_on) instead of the reference
+// grid.
+template <bool kList, class Visit>
 __device__ __forceinline__ void for_neighbour_cells(const DevParams& P, float3 r, uint32_t own, Visit visit)
 {
-    uint32_t c0, c1, c2;
-    if (P.hash_mode == NW_HASH_MASK) {
+    const bool coarse = kList && P.vl_on;
+    const uint32_t G0 = coarse ? P.lgrid[0] : P.grid[0];
+    const uint32_t G1 = coarse ? P.lgrid[1] : P.grid[1];
+    const uint32_t G2 = coarse ? P.lgrid[2] : P.grid[2];
+    uint32_t c0, c1, c2 = 0;
+    if (!coarse && P.hash_mode == NW_HASH_MASK) {
         const int3 g = grid_pos(P, r);
         c0 = cell_coord(P, 0, g.x);
         c1 = cell_coord(P, 1, g.y);
         c2 = cell_coord(P, 2, g.z);
     } else {
-        cell_of_hash(P, own, c0, c1, c2);
+        // modulo/clamp hash h = (c2 * G1 + c1) * G0 + c0, divided by multiply-shift
+        uint32_t rest = own;
+        if (G2 > 1u) {
+            c2 = fast_div(own, coarse ? P.ldiv_xy_m : P.div_gxy_m, coarse ? P.ldiv_xy_k : P.div_gxy_k);
+            rest = own - c2 * (G0 * G1);
+        }
+        c1 = fast_div(rest, coarse ? P.ldiv_x_m : P.div_gx_m, coarse ? P.ldiv_x_k : P.div_gx_k);
+        c0 = rest - c1 * G0;
     }
 #pragma unroll 1
     for (int dz = -1; dz <= 1; ++dz) {
         uint32_t z;
-        if (!nb_cell(P, 2, c2, dz, z)) continue;
+        if (!nb_cell((int)G2, P.bnd[2] == NW_PERIODIC, c2, dz, z)) continue;
 #pragma unroll 1
         for (int dy = -1; dy <= 1; ++dy) {
             uint32_t y;
-            if (!nb_cell(P, 1, c1, dy, y)) continue;
-            const uint32_t row = (z * P.grid[1] + y) * P.grid[0];
+            if (!nb_cell((int)G1, P.bnd[1] == NW_PERIODIC, c1, dy, y)) continue;
+            const uint32_t row = (z * G1 + y) * G0;
 #pragma unroll 1
             for (int dx = -1; dx <= 1; ++dx) {
                 uint32_t x;
-                if (!nb_cell(P, 0, c0, dx, x)) continue;
+                if (!nb_cell((int)G0, P.bnd[0] == NW_PERIODIC, c0, dx, x)) continue;
                 visit(row + x);
             }
         }

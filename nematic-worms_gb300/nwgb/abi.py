@@ -15,7 +15,7 @@ REPO_ROOT = PKG_ROOT.parent
 LIB_DIR = PKG_ROOT / "lib"
 LIB_PATH = LIB_DIR / "libnwgb.so"
 
-NW_ABI_VERSION = 1
+NW_ABI_VERSION = 2
 
 # status codes
 NW_OK = 0
@@ -32,13 +32,14 @@ NW_EFLAG_NONFINITE = 1 << 0
 NW_EFLAG_CELL_OVERFLOW = 1 << 1
 NW_EFLAG_TIMEOUT = 1 << 2
 NW_EFLAG_BAD_INDEX = 1 << 3
+NW_EFLAG_NEIGHBOR_OVERFLOW = 1 << 4
 
 NW_MODEL_WCA_WORMS = 0
 NW_MODEL_REF_DEM = 1
 NW_PERIODIC, NW_WALL, NW_WALL_NO_SLIP = 0, 1, 2
 NW_HASH_MODULO, NW_HASH_MASK = 0, 1
 NW_SRD_THERMO_NONE, NW_SRD_THERMO_REF_LAB, NW_SRD_THERMO_CELL_REL = 0, 1, 2
-NW_STRATEGY_AUTO, NW_STRATEGY_SORTED, NW_STRATEGY_CELL_LISTS = 0, 1, 2
+NW_STRATEGY_AUTO, NW_STRATEGY_SORTED, NW_STRATEGY_CELL_LISTS, NW_STRATEGY_VERLET = 0, 1, 2, 3
 
 NW_POSITION = 0
 NW_VELOCITY = 1
@@ -112,7 +113,9 @@ class NwConfig(C.Structure):
         ("dt", _f32),
         ("strategy", _i32),
         ("cell_capacity", _u32),
-        ("reserved", _u32 * 5),
+        ("neighbor_skin", _f32),
+        ("neighbor_capacity", _u32),
+        ("reserved", _u32 * 3),
     ]
 
     def copy(self) -> "NwConfig":
