@@ -88,14 +88,21 @@ def run_oracle(orc, cfg, pos, vel, tan, nsteps=1, prec=32):
 
 
 CASES = ["wca", "wca_srd", "wca_reverse", "ref", "ref_srd", "ref_walls"]
-STRATEGIES = [abi.NW_STRATEGY_CELL_LISTS, abi.NW_STRATEGY_SORTED]
+STRATEGIES = [abi.NW_STRATEGY_CELL_LISTS, abi.NW_STRATEGY_SORTED, abi.NW_STRATEGY_VERLET]
 # launches of one update: (bead step, SRD collision) + the step counter
-LAUNCHES = {abi.NW_STRATEGY_CELL_LISTS: (2, 8), abi.NW_STRATEGY_SORTED: (6, 8)}
+LAUNCHES = {abi.NW_STRATEGY_CELL_LISTS: (2, 8), abi.NW_STRATEGY_SORTED: (6, 8), abi.NW_STRATEGY_VERLET: (2, 8)}
+
+
+def strategy_applies(kind, strategy):
+    # Verlet lists serve the WCA law only (the REF_DEM pair set is cell-based)
+    return not (strategy == abi.NW_STRATEGY_VERLET and kind.startswith("ref"))
 
 
 @pytest.mark.parametrize("strategy", STRATEGIES)
 @pytest.mark.parametrize("kind", CASES)
 def test_one_step_matches_oracle(lib, orc, kind, strategy):
+    if not strategy_applies(kind, strategy):
+        pytest.skip("Verlet lists are WCA-only")
     cfg, pos, vel, tan = make_case(kind, lib)
     cfg.strategy = strategy
     g = run_gpu(cfg, pos, vel, tan)
@@ -125,6 +132,8 @@ def test_one_step_matches_oracle(lib, orc, kind, strategy):
 @pytest.mark.parametrize("strategy", STRATEGIES)
 @pytest.mark.parametrize("kind", ["wca", "ref_srd"])
 def test_graph_replay_is_bit_identical_to_direct_launches(lib, kind, strategy):
+    if not strategy_applies(kind, strategy):
+        pytest.skip("Verlet lists are WCA-only")
     cfg, pos, vel, tan = make_case(kind, lib)
     cfg.strategy = strategy
     a = run_gpu(cfg, pos, vel, tan, nsteps=12, graphs=True)
@@ -144,12 +153,50 @@ def test_strategies_agree(lib, kind):
     cfg, pos, vel, tan = make_case(kind, lib)
     out = []
     for strategy in STRATEGIES:
-        cfg.strategy = strategy
-        out.append(run_gpu(cfg, pos, vel, tan, nsteps=15, graphs=True))
-    for k in ("hash", "sorted_index", "cell_start"):
-        assert np.array_equal(out[0][k], out[1][k]), k
-    for k in ("pos", "vel", "force", "force_old", "tangent"):
-        assert rel_err(out[0][k], out[1][k]) < 1e-5, k
+        if strategy_applies(kind, strategy):
+            cfg.strategy = strategy
+            out.append(run_gpu(cfg, pos, vel, tan, nsteps=15, graphs=True))
+    for o in out[1:]:
+        for k in ("hash", "sorted_index", "cell_start"):
+            assert np.array_equal(out[0][k], o[k]), k
+        for k in ("pos", "vel", "force", "force_old", "tangent"):
+            assert rel_err(out[0][k], o[k]) < 1e-5, k
+
+
+@pytest.mark.parametrize("skin", [0.02, 0.3, 1.0])
+def test_verlet_lists_track_oracle_across_rebuilds(lib, orc, skin):
+    """A hot WCA system (kT = 2) moves far enough that lists are rebuilt
+    several times in 40 steps for the small skins and reused for the large
+    one; every step's forces must stay those of the full cell scan."""
+    cfg, pos, vel, tan = make_case("wca", lib)
+    cfg.kT = 2.0
+    cfg.strategy = abi.NW_STRATEGY_VERLET
+    cfg.neighbor_skin = skin
+    n = 40
+    g = run_gpu(cfg, pos, vel, tan, nsteps=n)
+    cfg.strategy = abi.NW_STRATEGY_SORTED
+    s = run_gpu(cfg, pos, vel, tan, nsteps=n)
+    # same dynamics as the reference-order path up to FP32 summation order
+    assert rel_err(g["pos"], s["pos"]) < 1e-5
+    assert rel_err(g["force"], s["force"]) < 1e-3
+    # the reference-grid hash of the Verlet system is computed when read
+    assert np.mean(g["hash"] == s["hash"]) > 0.999
+
+
+def test_verlet_list_overflow_is_reported(lib):
+    import nwgb
+
+    cfg, pos, vel, tan = make_case("wca", lib)
+    cfg.strategy = abi.NW_STRATEGY_VERLET
+    cfg.neighbor_capacity = 4
+    cfg.neighbor_skin = 3.0  # ~30 beads within the list radius
+    with nwgb.System(cfg) as s:
+        s.set_array(abi.NW_POSITION, pos)
+        s.set_array(abi.NW_VELOCITY, vel)
+        s.step(1, cfg.dt)
+        with pytest.raises(nwgb.NwError) as e:
+            s.sync()
+        assert e.value.status == abi.NW_ERR_CELL_OVERFLOW
 
 
 @pytest.mark.parametrize("kind", ["wca", "wca_srd", "ref"])
