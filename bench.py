@@ -39,6 +39,9 @@ WORKLOADS = {
     "wca_srd_400k": dict(k=1, layout="patches"),
     "wca_dense_2m": dict(k=2, layout="rows"),
     "wca_small_4k": dict(k=0, layout="patches"),
+    # 256 replicas of uneven size (50-2000 worms x 5-30 beads, F_act 0-2,
+    # k_bend 1-20, packing 0.3-0.6) in one batched launch per step
+    "batch_256": dict(batch=256),
 }
 
 
@@ -377,6 +380,110 @@ def run_ours(args):
     return 0
 
 
+def run_batch(args):
+    """Batched replicas: every step of all replicas in one launch, CUDA graphs of
+    100 steps, launch shape and neighbour search from the autotuner.  Reported
+    beside it: the same replicas run one by one through the single-system step
+    (sequential), and one single system holding as many beads (plain)."""
+    import math as _m
+
+    import torch
+
+    import nwgb
+    from nwgb import abi
+    from nwgb.init import batch_configs, initial_state, wca_config
+
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    R = WORKLOADS[args.workload]["batch"]
+    cfgs = batch_configs(R, seed=1000 * rank)
+    states = [initial_state(c, seed=r, layout="rows") for r, c in enumerate(cfgs)]
+    total = sum(c.n_beads for c in cfgs)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    chunk = 100
+    nchunks = max(1, args.steps // chunk)
+
+    def timed(step_fn, n):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(n):
+            step_fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1)
+
+    b = nwgb.Batch(cfgs)
+    b.set_stream(stream.cuda_stream)
+    for r, (pos, vel) in enumerate(states):
+        b.set_array(r, abi.NW_POSITION, pos)
+        b.set_array(r, abi.NW_VELOCITY, vel)
+    tune = b.autotune(trial_steps=20)
+    warm = 0
+    while warm < max(args.warmup, chunk):
+        b.step(chunk)
+        warm += chunk
+    b.sync()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ms = timed(lambda: b.step(chunk), nchunks)
+    clk = clocks.stop()
+    b.sync()
+    launches = b.last_launch_count * nchunks
+    value = total * chunk * nchunks / (ms / 1e3)
+    b.close()
+
+    # sequential: the same replicas one by one through the single-system step
+    seq_steps = chunk
+    seq_ms = 0.0
+    for r, c in enumerate(cfgs):
+        with nwgb.System(c) as s:
+            s.set_stream(stream.cuda_stream)
+            s.set_array(abi.NW_POSITION, states[r][0])
+            s.set_array(abi.NW_VELOCITY, states[r][1])
+            s.step(seq_steps, c.dt)
+            seq_ms += timed(lambda: s.step(seq_steps, c.dt), 1)
+            s.sync()
+    seq_value = total * seq_steps / (seq_ms / 1e3)
+
+    # plain: one system with the same number of beads at the mean packing
+    L = 20
+    M = int(round(total / L))
+    side = _m.sqrt(M * L * _m.pi / 4.0 / 0.45)
+    pc = wca_config(M, L, (side, side), activity=1.0, seed=1)
+    pp, pv = initial_state(pc, seed=1, layout="rows")
+    with nwgb.System(pc) as s:
+        s.set_stream(stream.cuda_stream)
+        s.set_array(abi.NW_POSITION, pp)
+        s.set_array(abi.NW_VELOCITY, pv)
+        s.step(chunk, pc.dt)
+        s.sync()
+        plain_ms = timed(lambda: s.step(chunk, pc.dt), nchunks)
+        s.sync()
+    plain_value = pc.n_beads * chunk * nchunks / (plain_ms / 1e3)
+
+    line = {"metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": world,
+            "steps": chunk * nchunks, "warmup": warm, "ms_per_step": ms / (chunk * nchunks),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "replicas": R, "beads": total, "model": "WCA_WORMS",
+                       "graph_steps": chunk, "parallelism": f"replicas x{world}",
+                       "tuning": {"threads_per_block": tune.threads_per_block, "strategy": int(tune.strategy),
+                                  "neighbor_skin": round(float(tune.neighbor_skin), 3),
+                                  "autotune_ms_per_step": float(tune.ms_per_step)},
+                       "l2": "state larger than L2 (no flush needed)"},
+            "clocks": clk, "gpu_launches": launches,
+            "sequential": {"value": seq_value, "steps": seq_steps,
+                           "path": "each replica alone: nw_step graphs of 100 steps, one after another"},
+            "plain": {"value": plain_value, "beads": pc.n_beads, "box": side,
+                      "path": "one single system of the same bead count (20-bead worms, packing 0.45)"},
+            "batched_over_plain": value / plain_value, "batched_over_sequential": value / seq_value}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -388,6 +495,12 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if "batch" in WORKLOADS[args.workload]:
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched replicas; "
+                              "its arm runs the single-system workloads"}), flush=True)
+            return 0
+        return run_batch(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -40,6 +40,7 @@ struct DevParams {
     uint32_t srd_ncells;
     float srd_cell[3];
     float srd_alpha, srd_kT, srd_shift_lo;
+    float srd_sin_a, srd_cos_a;  // sin and cos of the rotation angle alpha
     int32_t srd_rotate_beads, srd_thermo;
     uint32_t seed_lo, seed_hi;
     // multiply-shift divisors by grid[0] and grid[0] * grid[1] (see fast_div)

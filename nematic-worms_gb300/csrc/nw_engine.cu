@@ -60,6 +60,8 @@ DevParams make_dev_params(const NwConfig& c, float dt)
     P.langevin_on = (!c.srd_enabled || c.langevin_with_srd) ? 1 : 0;
     P.srd_on = c.srd_enabled;
     P.srd_alpha = c.srd_alpha;
+    P.srd_sin_a = (float)std::sin((double)c.srd_alpha);
+    P.srd_cos_a = (float)std::cos((double)c.srd_alpha);
     P.srd_kT = c.srd_kT;
     P.srd_shift_lo = c.srd_shift_lo;
     P.srd_rotate_beads = c.srd_rotate_beads;

@@ -19,6 +19,18 @@
 namespace nw {
 namespace {
 
+// Buffer k of a double / triple buffer by selects rather than an indexed
+// load: a StepBuffers copy in registers (the batch kernel's) stays there.
+template <class T>
+__device__ __forceinline__ T* pick2(T* const (&a)[2], uint32_t k)
+{
+    return k ? a[1] : a[0];
+}
+__device__ __forceinline__ uint32_t* pick3(uint32_t* const (&a)[3], uint32_t k)
+{
+    return k == 0u ? a[0] : (k == 1u ? a[1] : a[2]);
+}
+
 // Ascending bitonic sort of N (power of two) registers, fully unrolled.
 template <int N>
 __device__ __forceinline__ void bitonic_sort(uint32_t (&a)[N])
@@ -203,7 +215,8 @@ __device__ __forceinline__ float vl_bound(const StepBuffers& S, unsigned long lo
 
 // Verlet pair force: the bead's list from the last build, each pair still
 // tested against lj_rcut.  Pairs are summed in list order, which is the
-// cell-scan order of the build.
+// cell-scan order of the build.  Neighbours are fetched four at a time so
+// that four index loads, then four position gathers, are in flight together.
 __device__ __forceinline__ float3 verlet_force(const DevParams& P, const StepBuffers& S,
                                                const float4* __restrict__ pos, uint32_t i, float3 r)
 {
@@ -211,16 +224,25 @@ __device__ __forceinline__ float3 verlet_force(const DevParams& P, const StepBuf
     if (k > P.vl_cap) k = P.vl_cap;
     float3 f = zero3();
     const uint32_t* __restrict__ col = S.nbr + i;
-    for (uint32_t m = 0; m < k; ++m) {
-        const uint32_t j = __ldg(col + (size_t)m * P.nb);
-        float3 dr = f3(__ldg(pos + j)) - r;
-        min_image(P, dr);
-        const float rr = dot3(dr, dr);
-        if (rr > P.lj_rc2) continue;
-        const float fm = wca_lj(P, rr);
-        f.x -= fm * dr.x;
-        f.y -= fm * dr.y;
-        f.z -= fm * dr.z;
+    for (uint32_t m = 0; m < k; m += 4) {
+        uint32_t j[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) j[q] = m + q < k ? __ldg(col + (size_t)(m + q) * P.nb) : i;
+        float4 pj[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) pj[q] = __ldg(pos + j[q]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (m + q >= k) break;
+            float3 dr = f3(pj[q]) - r;
+            min_image(P, dr);
+            const float rr = dot3(dr, dr);
+            if (rr > P.lj_rc2) continue;
+            const float fm = wca_lj(P, rr);
+            f.x -= fm * dr.x;
+            f.y -= fm * dr.y;
+            f.z -= fm * dr.z;
+        }
     }
     return f;
 }
@@ -275,23 +297,24 @@ __device__ __forceinline__ void vl_commit(const StepBuffers& S, unsigned long lo
 }
 
 // Pair force of bead i for update n (reads the update-n buffers and list).
+// blk = the block's index among the blocks of its system.
 template <int CAP, bool kRef>
 __device__ __forceinline__ float3 list_pair_force(const DevParams& P, const StepBuffers& S, unsigned long long n,
-                                                  uint32_t i)
+                                                  uint32_t i, uint32_t blk)
 {
     const uint32_t cur = (uint32_t)(n & 1ull);
-    const uint32_t* cnt = S.lcount[(uint32_t)(n % 3ull)];
-    const uint32_t* slots = S.lslot[cur];
-    const float3 r = f3(S.pos2[cur][i]);
-    if (kRef) return ref_list_force<CAP>(P, S.pos2[cur], S.vel2[cur], S.tan2[cur], cnt, slots, i, r);
+    const uint32_t* cnt = pick3(S.lcount, (uint32_t)(n % 3ull));
+    const uint32_t* slots = pick2(S.lslot, cur);
+    const float3 r = f3(pick2(S.pos2, cur)[i]);
+    if (kRef) return ref_list_force<CAP>(P, pick2(S.pos2, cur), pick2(S.vel2, cur), pick2(S.tan2, cur), cnt, slots, i, r);
     if (P.vl_on) {
         const float bound = vl_bound(S, n);
         const bool rebuild = !(bound <= P.vl_half_skin);  // a NaN bound rebuilds too
-        if (blockIdx.x == 0 && threadIdx.x == 0) vl_commit(S, n, rebuild, bound);
-        if (!rebuild) return verlet_force(P, S, S.pos2[cur], i, r);
-        return verlet_build_force<CAP>(P, S, S.pos2[cur], cnt, slots, i, r, S.hash2[cur][i]);
+        if (blk == 0 && threadIdx.x == 0) vl_commit(S, n, rebuild, bound);
+        if (!rebuild) return verlet_force(P, S, pick2(S.pos2, cur), i, r);
+        return verlet_build_force<CAP>(P, S, pick2(S.pos2, cur), cnt, slots, i, r, pick2(S.hash2, cur)[i]);
     }
-    return wca_list_force<CAP>(P, S.pos2[cur], cnt, slots, i, r, S.hash2[cur][i]);
+    return wca_list_force<CAP>(P, pick2(S.pos2, cur), cnt, slots, i, r, pick2(S.hash2, cur)[i]);
 }
 
 // Shared-memory bytes of the pro part for a block of `beads` beads.
@@ -301,31 +324,33 @@ __host__ __device__ __forceinline__ size_t pro_smem(uint32_t beads, bool reverse
 }
 
 // pro(n) for the block's filaments: every thread of the block must call it.
-// fprev = F_{n-1} of this thread's bead (complete force of the previous update).
+// fprev = F_{n-1} of this thread's bead (complete force of the previous update);
+// blk / nblk = the block's index among, and the number of, its system's blocks.
 template <int CAP>
 __device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& S, unsigned long long n, float dt,
-                                         uint32_t fpb, bool active, uint32_t i, float3 fprev)
+                                         uint32_t fpb, bool active, uint32_t i, float3 fprev, uint32_t blk,
+                                         uint32_t nblk)
 {
     extern __shared__ float4 sm[];
     const uint32_t L = P.L;
     const uint32_t beads = fpb * L;
     const uint32_t t = threadIdx.x;
-    const uint32_t w0 = blockIdx.x * fpb;
+    const uint32_t w0 = blk * fpb;
     const uint32_t in = (uint32_t)((n + 1ull) & 1ull), out = (uint32_t)(n & 1ull);
     float4* smp = sm;                                       // positions [beads]
     float4* smx = sm + (P.reverse_on ? 3u : 1u) * beads;    // triple forces [3][beads]
 
     // lists of update n+1 must start empty: clear them while nobody reads them
     {
-        uint32_t* nxt = S.lcount[(uint32_t)((n + 1ull) % 3ull)];
-        const uint32_t stride = gridDim.x * blockDim.x;
-        for (uint32_t c = blockIdx.x * blockDim.x + t; c < P.lncells; c += stride) nxt[c] = 0u;
+        uint32_t* nxt = pick3(S.lcount, (uint32_t)((n + 1ull) % 3ull));
+        const uint32_t stride = nblk * blockDim.x;
+        for (uint32_t c = blk * blockDim.x + t; c < P.lncells; c += stride) nxt[c] = 0u;
     }
 
     float4 nP = make_float4(0.f, 0.f, 0.f, 0.f), nV = nP, nFo = nP;
     float disp2 = 0.f;  // squared displacement of this update (Verlet list bound)
     if (active) {
-        const float4 P4 = S.pos2[in][i], V4 = S.vel2[in][i], Fo4 = S.force_old[i];
+        const float4 P4 = pick2(S.pos2, in)[i], V4 = pick2(S.vel2, in)[i], Fo4 = S.force_old[i];
         float3 p = f3(P4), v = f3(V4);
         const float3 f = fprev, fo = f3(Fo4);
         // velocity Verlet (particles_kernel_impl.cuh:93-97)
@@ -414,17 +439,17 @@ __device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& 
         if (c > 0) wca_bond(P, me, f3(R[c - 1]), fs);
         if (c + 1 < L) wca_bond_drive(P, me, f3(R[c + 1]), fs);
     }
-    S.pos2[out][i] = nP;
-    S.vel2[out][i] = nV;
+    pick2(S.pos2, out)[i] = nP;
+    pick2(S.vel2, out)[i] = nV;
     S.force_old[i] = nFo;
     S.force[i] = make_float4(fs.x, fs.y, fs.z, 0.f);
-    S.tan2[out][i] = wt ? make_float4(tg.x, tg.y, tg.z, 0.f) : S.tan2[in][i];
+    pick2(S.tan2, out)[i] = wt ? make_float4(tg.x, tg.y, tg.z, 0.f) : pick2(S.tan2, in)[i];
     if (!finite3(f3(nP)) || !finite3(fs)) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
 
     const uint32_t h = P.vl_on ? list_hash(P, f3(nP)) : bead_hash(P, f3(nP));
-    S.hash2[out][i] = h;
-    const uint32_t slot = atomicAdd(&S.lcount[(uint32_t)(n % 3ull)][h], 1u);
-    if (slot < (uint32_t)CAP) S.lslot[out][(size_t)h * CAP + slot] = i;
+    pick2(S.hash2, out)[i] = h;
+    const uint32_t slot = atomicAdd(&pick3(S.lcount, (uint32_t)(n % 3ull))[h], 1u);
+    if (slot < (uint32_t)CAP) pick2(S.lslot, out)[(size_t)h * CAP + slot] = i;
     else atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
 }
 
@@ -436,7 +461,7 @@ __global__ void __launch_bounds__(MAXT) bead_pro_kernel(const DevParams P, const
     const uint32_t i = blockIdx.x * fpb * P.L + threadIdx.x;
     const bool active = threadIdx.x < fpb * P.L && i < P.nb;
     const float3 fprev = active ? f3(S.force[i]) : zero3();
-    pro_part<CAP>(P, S, n, dt, fpb, active, i, fprev);
+    pro_part<CAP>(P, S, n, dt, fpb, active, i, fprev, blockIdx.x, gridDim.x);
 }
 
 template <int CAP, bool kRef>
@@ -445,7 +470,7 @@ __global__ void __launch_bounds__(256) bead_epi_kernel(const DevParams P, const 
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.nb) return;
     const unsigned long long n = *S.step_base + off;
-    const float3 pair = list_pair_force<CAP, kRef>(P, S, n, i);
+    const float3 pair = list_pair_force<CAP, kRef>(P, S, n, i, blockIdx.x);
     float4 F = S.force[i];
     F.x += pair.x;
     F.y += pair.y;
@@ -464,17 +489,91 @@ __global__ void __launch_bounds__(MAXT) bead_fused_kernel(const DevParams P, con
     const bool active = threadIdx.x < fpb * P.L && i < P.nb;
     float3 Fn = zero3();
     if (active) {
-        const float3 pair = list_pair_force<CAP, kRef>(P, S, n, i);
+        const float3 pair = list_pair_force<CAP, kRef>(P, S, n, i, blockIdx.x);
         const float4 F = S.force[i];
         Fn = make_float3(F.x + pair.x, F.y + pair.y, F.z + pair.z);
         if (!finite3(Fn)) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
     }
-    pro_part<CAP>(P, S, n + 1ull, dt, fpb, active, i, Fn);
+    pro_part<CAP>(P, S, n + 1ull, dt, fpb, active, i, Fn, blockIdx.x, gridDim.x);
+}
+
+// A batch block: copy its replica's parameter block into shared memory and
+// run pro, epi or fused for that replica's slice of the batch buffers.
+template <int CAP, int MODE, int MAXT>
+__global__ void __launch_bounds__(MAXT) batch_kernel(const ReplicaSlot* __restrict__ table,
+                                                     const uint32_t* __restrict__ block_rep, const StepBuffers S0,
+                                                     uint32_t off)
+{
+    __shared__ DevParams sP;
+    const uint32_t r = __ldg(block_rep + blockIdx.x);
+    const ReplicaSlot* e = table + r;
+    {
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(&e->P);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(&sP);
+        for (uint32_t w = threadIdx.x; w < (uint32_t)(sizeof(DevParams) / 4); w += blockDim.x) dst[w] = __ldg(src + w);
+    }
+    __syncthreads();
+    const DevParams& P = sP;
+    const uint32_t bo = e->bead_off, co = e->cell_off, blk = blockIdx.x - e->blk0, nblk = e->nblk, fpb = e->fpb;
+    const float dt = e->dt;
+    StepBuffers S = S0;
+    for (int k = 0; k < 2; ++k) {
+        S.pos2[k] += bo;
+        S.vel2[k] += bo;
+        S.tan2[k] += bo;
+        S.hash2[k] += bo;
+        S.lslot[k] += (size_t)co * CAP;
+    }
+    for (int k = 0; k < 3; ++k) S.lcount[k] += co;
+    S.force += bo;
+    S.force_old += bo;
+    if (S.nbr) S.nbr += e->nbr_off;
+    if (S.nnb) S.nnb += bo;
+    if (S.vstate) S.vstate += 8u * r;
+    const unsigned long long n = *S.step_base + off;
+    const uint32_t i = blk * fpb * P.L + threadIdx.x;
+    const bool active = threadIdx.x < fpb * P.L && i < P.nb;
+    if (MODE == kBatchPro) {
+        const float3 fprev = active ? f3(S.force[i]) : zero3();
+        pro_part<CAP>(P, S, n, dt, fpb, active, i, fprev, blk, nblk);
+        return;
+    }
+    float3 Fn = zero3();
+    if (active) {
+        const float3 pair = list_pair_force<CAP, false>(P, S, n, i, blk);
+        const float4 F = S.force[i];
+        Fn = make_float3(F.x + pair.x, F.y + pair.y, F.z + pair.z);
+        if (!finite3(Fn)) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
+        if (MODE == kBatchEpi) S.force[i] = make_float4(Fn.x, Fn.y, Fn.z, F.w);
+    }
+    if (MODE == kBatchFused) pro_part<CAP>(P, S, n + 1ull, dt, fpb, active, i, Fn, blk, nblk);
 }
 
 uint32_t cdiv32(uint64_t a, uint32_t b) { return (uint32_t)((a + b - 1) / b); }
 
 }  // namespace
+
+void launch_batch(int mode, const ReplicaSlot* table, const uint32_t* block_rep, uint32_t blocks, uint32_t threads,
+                  size_t smem, uint32_t cap, const StepBuffers& S, uint32_t off, cudaStream_t s)
+{
+    if (blocks == 0) return;
+    const bool big = threads > 256;
+#define NW_BATCH(CAPV, MODEV)                                                                                  \
+    do {                                                                                                       \
+        if (big) batch_kernel<CAPV, MODEV, 512><<<blocks, threads, smem, s>>>(table, block_rep, S, off);      \
+        else batch_kernel<CAPV, MODEV, 256><<<blocks, threads, smem, s>>>(table, block_rep, S, off);          \
+    } while (0)
+#define NW_BATCH_MODE(CAPV)                                    \
+    do {                                                       \
+        if (mode == kBatchPro) NW_BATCH(CAPV, kBatchPro);      \
+        else if (mode == kBatchEpi) NW_BATCH(CAPV, kBatchEpi); \
+        else NW_BATCH(CAPV, kBatchFused);                      \
+    } while (0)
+    if (cap == 16) NW_BATCH_MODE(16);
+    else NW_BATCH_MODE(8);
+#undef NW_BATCH_MODE
+#undef NW_BATCH
+}
 
 uint32_t list_filaments_per_block(uint32_t L, uint32_t nf)
 {

@@ -15,4 +15,28 @@ uint64_t launch_bead_epi(const DevParams& P, const StepBuffers& B, uint32_t off,
 // epi(n) followed by pro(n+1) in one kernel.
 uint64_t launch_bead_fused(const DevParams& P, const StepBuffers& B, uint32_t off, float dt, cudaStream_t s);
 
+// ---- batched replicas (nw_batch.cu) ------------------------------------------
+
+// One replica of a batch as its blocks see it: its parameter block and where
+// its beads, list cells, neighbour lists and blocks start in the batch's
+// concatenated buffers.
+struct ReplicaSlot {
+    DevParams P;
+    float dt;
+    uint32_t bead_off;  // first bead
+    uint32_t cell_off;  // first list cell
+    uint32_t blk0;      // first block of the launch
+    uint32_t nblk;      // blocks of this replica
+    uint32_t fpb;       // filaments per block
+    uint32_t pad[2];
+    unsigned long long nbr_off;  // first neighbour-list word
+};
+
+enum BatchMode { kBatchPro = 0, kBatchEpi = 1, kBatchFused = 2 };
+
+// One launch over all replicas: block b serves replica block_rep[b].  S holds
+// the batch's base pointers; `threads` >= every replica's fpb * L.
+void launch_batch(int mode, const ReplicaSlot* table, const uint32_t* block_rep, uint32_t blocks, uint32_t threads,
+                  size_t smem, uint32_t cap, const StepBuffers& S, uint32_t off, cudaStream_t s);
+
 }  // namespace nw

@@ -282,14 +282,27 @@ __global__ void __launch_bounds__(256) srd_scatter_kernel(const DevParams P, con
 // (particles_kernel_impl.cuh:605-637) or none, the mass-weighted cell mean
 // (:560-594), the +/- alpha rotation of (v - u) (:640-691), the
 // relative-velocity thermostat when selected, and the solvent's ballistic
-// streaming by dt_srd (solvent_integrator, :145-205).  Velocities are read
-// once per pass from the pre-collision buffers and written once: beads in
-// place, solvent to the other solvent buffer at its new position in cell
-// order.
-__global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
-                                                          float dt_srd, uint32_t buf_sel)
+// streaming by dt_srd (solvent_integrator, :145-205).  Beads are written in
+// place, the solvent to the other solvent buffer at its new position in
+// cell order.
+//
+// Memory: each thread sorts its member ids in its own shared-memory column
+// ([slot][thread], conflict-free) and keeps the first kSrdVel member
+// velocities there too, so every velocity is gathered from global memory
+// once; positions are gathered once, in the final pass.  Cells with more
+// than kSrdIds members (a Poisson tail at the usual densities) rank their
+// members in global memory instead.
+constexpr int kSrdThreads = 256;
+constexpr uint32_t kSrdIds = 16;
+constexpr uint32_t kSrdVel = 8;
+
+__global__ void __launch_bounds__(kSrdThreads) srd_collide_kernel(const DevParams P, const StepBuffers S,
+                                                                  uint32_t step_off, float dt_srd, uint32_t buf_sel)
 {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ uint32_t s_ids[kSrdIds][kSrdThreads];
+    __shared__ float4 s_vel[kSrdVel][kSrdThreads];
+    const uint32_t t = threadIdx.x;
+    const uint32_t c = blockIdx.x * blockDim.x + t;
     if (c >= P.srd_ncells) return;
     const unsigned long long step = *S.step_base + step_off;
     const uint32_t cur = buf_sel < 2u ? buf_sel : (uint32_t)(step & 1ull);
@@ -308,20 +321,19 @@ __global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, con
     float3 u = zero3();
     if (n > 0) {
         // members in stable order: ids < nb are beads, nb + k is solvent k
-        uint32_t ids[kSrdLocal];
-        const bool local = n <= kSrdLocal;
+        const bool local = n <= kSrdIds;
         if (n > kStableCap) atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
         if (local) {
             for (uint32_t k = 0; k < n; ++k) {
                 const uint32_t x = k < nbc ? S.srd_btmp[b0 + k] : P.nb + S.srd_stmp[s0 + (k - nbc)];
                 uint32_t m = k;
-                while (m > 0 && ids[m - 1] > x) {
-                    ids[m] = ids[m - 1];
+                while (m > 0 && s_ids[m - 1][t] > x) {
+                    s_ids[m][t] = s_ids[m - 1][t];
                     --m;
                 }
-                ids[m] = x;
+                s_ids[m][t] = x;
             }
-            for (uint32_t k = 0; k < n; ++k) S.srd_sorted_index[start + k] = ids[k];
+            for (uint32_t k = 0; k < n; ++k) S.srd_sorted_index[start + k] = s_ids[k][t];
         } else {
             for (uint32_t q = b0; q < b1; ++q) {
                 const uint32_t x = S.srd_btmp[q];
@@ -334,24 +346,24 @@ __global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, con
                 S.srd_sorted_index[start + nbc + r] = P.nb + x;
             }
         }
-        auto member = [&](uint32_t k) -> uint32_t { return local ? ids[k] : S.srd_sorted_index[start + k]; };
-        auto vel_of = [&](uint32_t id) -> float4 { return id < P.nb ? bvel[id] : sv_old[id - P.nb]; };
-        // reference isokinetic rule: lambda scales every member before the mean
-        float lam1 = 1.0f;
+        auto member = [&](uint32_t k) -> uint32_t { return local ? s_ids[k][t] : S.srd_sorted_index[start + k]; };
+        auto gather = [&](uint32_t id) -> float4 { return id < P.nb ? bvel[id] : sv_old[id - P.nb]; };
+        // velocity of member k: gathered once, then from the shared-memory cache
+        auto vel_at = [&](uint32_t k) -> float4 { return k < kSrdVel ? s_vel[k][t] : gather(member(k)); };
         const bool lab = P.srd_thermo == NW_SRD_THERMO_REF_LAB;
-        if (lab) {
-            float E = 0.f;
-            for (uint32_t k = 0; k < n; ++k) {
-                const float4 V = vel_of(member(k));
-                const float3 v = f3(V);
-                E += (0.5f * V.w) * dot3(v, v);
-            }
-            lam1 = sqrtf(P.srd_kT / E);
+        float E = 0.f;
+        for (uint32_t k = 0; k < n; ++k) {
+            const float4 V = gather(member(k));
+            if (k < kSrdVel) s_vel[k][t] = V;
+            const float3 v = f3(V);
+            E += (0.5f * V.w) * dot3(v, v);
         }
+        // reference isokinetic rule: lambda scales every member before the mean
+        const float lam1 = lab ? sqrtf(P.srd_kT / E) : 1.0f;
         auto scaled = [&](float4 V) -> float3 { return lab ? make_float3(lam1 * V.x, lam1 * V.y, lam1 * V.z) : f3(V); };
         float M = 0.f;
         for (uint32_t k = 0; k < n; ++k) {
-            const float4 V = vel_of(member(k));
+            const float4 V = vel_at(k);
             u += V.w * scaled(V);
             M += V.w;
         }
@@ -359,9 +371,9 @@ __global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, con
             const float inv = 1.0f / M;
             u = u * inv;
         }
-        const int sign = 2 * (int)(u01(rng_draw(P, c, step, kRngSrdRot).x) > 0.5f) - 1;
-        const float ang = (float)sign * P.srd_alpha;
-        const float sa = sinf(ang), ca = cosf(ang);
+        // rotation by +alpha or -alpha with equal probability
+        const bool plus = u01(rng_draw(P, c, step, kRngSrdRot).x) > 0.5f;
+        const float sa = plus ? P.srd_sin_a : -P.srd_sin_a, ca = P.srd_cos_a;
         const bool rel = P.srd_thermo == NW_SRD_THERMO_CELL_REL;
         float lam2 = 1.0f;
         bool scale2 = false;
@@ -369,9 +381,8 @@ __global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, con
             uint32_t nrot = 0;
             float ke = 0.f;
             for (uint32_t k = 0; k < n; ++k) {
-                const uint32_t id = member(k);
-                if (id < P.nb && !P.srd_rotate_beads) continue;
-                const float4 V = vel_of(id);
+                if (member(k) < P.nb && !P.srd_rotate_beads) continue;
+                const float4 V = vel_at(k);
                 const float3 d = scaled(V) - u;
                 const float rx = d.x * ca - d.y * sa;
                 const float ry = d.x * sa + d.y * ca;
@@ -386,7 +397,7 @@ __global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, con
         for (uint32_t k = 0; k < n; ++k) {
             const uint32_t id = member(k);
             const bool is_bead = id < P.nb;
-            const float4 V = vel_of(id);
+            const float4 V = vel_at(k);
             float3 v = scaled(V);
             if (!is_bead || P.srd_rotate_beads) {
                 const float3 d = v - u;

@@ -22,7 +22,6 @@ namespace nw {
 // processed with bounded work; physical states never get close.
 constexpr uint32_t kStableCap = 128;  // members ordered exactly up to this count
 constexpr uint32_t kPairCap = 1024;   // members scanned per neighbour cell
-constexpr uint32_t kSrdLocal = 32;    // SRD members kept in registers
 
 struct StepBuffers {
     // Bead state.  pos2/vel2/tan2/hash2 are double buffers: the cell-list path

@@ -237,6 +237,34 @@ LEGACY_API = [
 _lib = None
 
 
+class NwBatchTuning(C.Structure):
+    """include/nwgb_batch.h NwBatchTuning."""
+
+    _fields_ = [("threads_per_block", _u32), ("strategy", C.c_int32), ("neighbor_skin", _f32),
+                ("ms_per_step", _f32)]
+
+
+_bp = C.c_void_p
+BATCH_API = [
+    ("nw_batch_create", C.c_int, [C.POINTER(NwConfig), C.c_int, C.POINTER(_bp)]),
+    ("nw_batch_destroy", C.c_int, [_bp]),
+    ("nw_batch_counts", C.c_int, [_bp, C.POINTER(C.c_int), C.POINTER(C.c_uint64)]),
+    ("nw_batch_replica", C.c_int, [_bp, C.c_int, C.POINTER(_u32), C.POINTER(C.c_uint64)]),
+    ("nw_batch_set_array", C.c_int, [_bp, C.c_int, C.c_int, _P, _u32, _u32]),
+    ("nw_batch_get_array", C.c_int, [_bp, C.c_int, C.c_int, _P, _u32, _u32]),
+    ("nw_batch_device_array", C.c_int, [_bp, C.c_int, C.POINTER(_P)]),
+    ("nw_batch_step", C.c_int, [_bp, C.c_int]),
+    ("nw_batch_sync", C.c_int, [_bp]),
+    ("nw_batch_set_stream", C.c_int, [_bp, _P]),
+    ("nw_batch_set_graphs", C.c_int, [_bp, C.c_int]),
+    ("nw_batch_get_step", C.c_uint64, [_bp]),
+    ("nw_batch_last_launch_count", C.c_int, [_bp, C.POINTER(C.c_uint64)]),
+    ("nw_batch_get_tuning", C.c_int, [_bp, C.POINTER(NwBatchTuning)]),
+    ("nw_batch_set_tuning", C.c_int, [_bp, C.POINTER(NwBatchTuning)]),
+    ("nw_batch_autotune", C.c_int, [_bp, C.c_int, C.POINTER(NwBatchTuning)]),
+]
+
+
 def load_library(path: os.PathLike | str | None = None) -> C.CDLL:
     """Load libnwgb.so (once) and declare every exported function.
 
@@ -252,7 +280,7 @@ def load_library(path: os.PathLike | str | None = None) -> C.CDLL:
             f"{p} is missing: build the CUDA library first (python -c 'import __graft_entry__ as g; g.build()')"
         )
     lib = C.CDLL(str(p))
-    for name, res, args in HANDLE_API + LEGACY_API:
+    for name, res, args in HANDLE_API + LEGACY_API + BATCH_API:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args

@@ -67,6 +67,25 @@ def baseline_config(k: int, lib=None, seed: int = 0) -> NwConfig:
     raise ValueError(k)
 
 
+def batch_configs(n_replicas: int = 256, seed: int = 0, lib=None, worms=(50, 2000), beads=(5, 30),
+                  activity=(0.0, 2.0), bend_k=(1.0, 20.0), packing=(0.3, 0.6)) -> list:
+    """Replicas of uneven size for the batched engine: per replica worm count
+    and length uniform in the given integer ranges, F_act, k_bend and packing
+    fraction uniform in theirs, box side sqrt(N pi/4 / packing) for N beads of
+    unit diameter, seed = seed + r."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for r in range(n_replicas):
+        M = int(rng.integers(worms[0], worms[1] + 1))
+        L = int(rng.integers(beads[0], beads[1] + 1))
+        phi = float(rng.uniform(*packing))
+        side = math.sqrt(M * L * math.pi / 4.0 / phi)
+        c = wca_config(M, L, (side, side), activity=float(rng.uniform(*activity)),
+                       bend_k=float(rng.uniform(*bend_k)), seed=seed + r, lib=lib)
+        out.append(c)
+    return out
+
+
 def _worm_beads(head, angle, L, spacing):
     d = np.array([math.cos(angle), math.sin(angle)])
     return head[None, :] + np.arange(L)[:, None] * spacing * d[None, :]
