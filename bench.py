@@ -42,6 +42,9 @@ WORKLOADS = {
     # 256 replicas of uneven size (50-2000 worms x 5-30 beads, F_act 0-2,
     # k_bend 1-20, packing 0.3-0.6) in one batched launch per step
     "batch_256": dict(batch=256),
+    # 64 replicas of the 4k-bead workload, 200-step differentiable rollout,
+    # lists frozen per 20-step segment, gradient of the S / C_v loss
+    "adjoint_64x4k": dict(adjoint=64),
 }
 
 
@@ -484,6 +487,82 @@ def run_batch(args):
     return 0
 
 
+def run_adjoint(args):
+    """Differentiable rollout: forward + adjoint of 200 steps for 64 replicas of
+    the 4k-bead workload (FP32), timed on the device; beside it the production
+    batched step on the same replicas and steps."""
+    import numpy as np
+    import torch
+
+    import nwgb
+    from nwgb import abi
+    from nwgb.adjoint import Rollout, rollout
+    from nwgb.init import baseline_config, initial_state
+    from nwgb.observables import PairSample, loss_s_cv, velocity_correlation
+
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    R = WORKLOADS[args.workload]["adjoint"]
+    H, SEG = 200, 20
+    cfg = baseline_config(0, seed=7)
+    states = [initial_state(cfg, seed=r, layout="patches") for r in range(R)]
+    pos = torch.from_numpy(np.concatenate([s[0] for s in states])).cuda()
+    vel = torch.from_numpy(np.concatenate([s[1] for s in states])).cuda()
+    ro = Rollout(cfg, R, H, SEG, 32)
+    ro.set_state(pos, vel)
+    box = [cfg.box[0], cfg.box[1], cfg.box[2]]
+    pairs = PairSample(R, cfg.n_beads, 20000, seed=1, device="cuda")
+    # C_target from a seeded run at the reference parameters
+    with torch.no_grad():
+        p, v = ro.forward([1.0, 10.0, 57.0, 0.5])
+        target = velocity_correlation(p[:, :3].reshape(R, -1, 3).double(), v[:, :3].reshape(R, -1, 3).double(),
+                                      pairs, box).mean(0, keepdim=True)
+    fwd, bwd = [], []
+    reps = max(3, min(10, args.steps // H))
+    for k in range(args.warmup + reps):
+        th = torch.tensor([1.1, 8.0, 50.0, 0.8], dtype=torch.float64, requires_grad=True)
+        p, v = rollout(th, ro)
+        L = loss_s_cv(p[:, :3].reshape(R, -1, 3).double(), v[:, :3].reshape(R, -1, 3).double(), cfg.filament_size,
+                      box, pairs, target)
+        L.backward()
+        f_ms, b_ms = ro.timings()
+        if k >= args.warmup:
+            fwd.append(f_ms)
+            bwd.append(b_ms)
+    f_ms, b_ms = statistics.median(fwd), statistics.median(bwd)
+    ro.close()
+    # production step on the same replicas (batched engine, one launch per step)
+    cfgs = [baseline_config(0, seed=7 + r) for r in range(R)]
+    stream = torch.cuda.Stream()
+    with nwgb.Batch(cfgs) as b:
+        b.set_stream(stream.cuda_stream)
+        for r, (ps, vs) in enumerate(states):
+            b.set_array(r, abi.NW_POSITION, ps)
+            b.set_array(r, abi.NW_VELOCITY, vs)
+        b.step(H)
+        b.sync()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        b.step(H)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        prod_ms = ev0.elapsed_time(ev1)
+    nbt = R * cfg.n_beads
+    line = {"metric": "bead-steps/s", "value": nbt * H / ((f_ms + b_ms) / 1e3), "unit": "bead-steps/s",
+            "n_gpus": world, "steps": H * len(fwd), "warmup": args.warmup, "ms_per_step": (f_ms + b_ms) / H,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "replicas": R, "beads": nbt, "horizon": H, "segment": SEG,
+                       "loss": "(S2 - 0.7)^2 + |C_v - C_target|^2, 32 bins"},
+            "adjoint": {"forward_ms": f_ms, "backward_ms": b_ms, "backward_over_forward": b_ms / f_ms,
+                        "gradient_over_production_step": (f_ms + b_ms) / prod_ms,
+                        "production_batched_ms": prod_ms,
+                        "note": "forward = the rollout's own frozen-list step (with checkpoints); "
+                                "production = the batched engine over the same replicas and steps"}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -495,6 +574,11 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if "adjoint" in WORKLOADS[args.workload]:
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no gradients"}), flush=True)
+            return 0
+        return run_adjoint(args)
     if "batch" in WORKLOADS[args.workload]:
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched replicas; "

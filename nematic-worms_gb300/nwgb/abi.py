@@ -265,6 +265,18 @@ BATCH_API = [
 ]
 
 
+_ap = C.c_void_p
+ADJOINT_API = [
+    ("nw_adj_create", C.c_int, [C.POINTER(NwConfig), C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(_ap)]),
+    ("nw_adj_destroy", C.c_int, [_ap]),
+    ("nw_adj_set_stream", C.c_int, [_ap, _P]),
+    ("nw_adj_set_state", C.c_int, [_ap, _P, _P]),
+    ("nw_adj_forward", C.c_int, [_ap, C.POINTER(C.c_double), _P, _P]),
+    ("nw_adj_backward", C.c_int, [_ap, _P, _P, C.POINTER(C.c_double)]),
+    ("nw_adj_timings", C.c_int, [_ap, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+]
+
+
 def load_library(path: os.PathLike | str | None = None) -> C.CDLL:
     """Load libnwgb.so (once) and declare every exported function.
 
@@ -280,7 +292,7 @@ def load_library(path: os.PathLike | str | None = None) -> C.CDLL:
             f"{p} is missing: build the CUDA library first (python -c 'import __graft_entry__ as g; g.build()')"
         )
     lib = C.CDLL(str(p))
-    for name, res, args in HANDLE_API + LEGACY_API + BATCH_API:
+    for name, res, args in HANDLE_API + LEGACY_API + BATCH_API + ADJOINT_API:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
