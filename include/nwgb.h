@@ -54,7 +54,8 @@ enum {
     NW_ERR_TIMEOUT = 5,       /* a bounded device wait gave up */
     NW_ERR_NOMEM = 6,         /* device or host allocation failed */
     NW_ERR_UNSUPPORTED = 7,   /* feature not available in this configuration */
-    NW_ERR_NO_DEVICE = 8      /* no CUDA device visible */
+    NW_ERR_NO_DEVICE = 8,     /* no CUDA device visible */
+    NW_ERR_IO = 9             /* a file could not be opened or written */
 };
 
 /* Device error word bits (read with nw_error_word). */
@@ -293,6 +294,28 @@ typedef struct NwKernelTime {
     uint64_t launches;
 } NwKernelTime;
 nw_status nw_profile_steps(nw_system* sys, int nsteps, float dt, NwKernelTime* out, int max_entries, int* n_entries);
+
+/* ---- trajectory output ---------------------------------------------------- */
+
+/* Frames in the reference's text format (ParticleSystem::writeOutputs,
+ * simulation/particleSystem.cpp:481-532, read by analysis/afa/io.py:4-25):
+ * a line with the particle count, a line with the parameters as a JSON
+ * object, then one line per particle, "A x y z vx vy vz" for beads and
+ * "B x y z vx vy vz" for solvent (floats as C++ streams print them, 6
+ * significant digits).  Unlike the reference, the frame leaves the step
+ * loop at once: nw_writer_frame enqueues a device-to-device snapshot of the
+ * state on the system's stream, the writer copies it to pinned host memory
+ * on its own stream, and a writer thread formats and appends it to the
+ * file.  Two frames can be in flight; a third call waits for the oldest.
+ * Close every writer before destroying its system. */
+typedef struct nw_writer nw_writer;
+nw_status nw_writer_open(nw_system* sys, const char* path, int append, nw_writer** out);
+/* Snapshot of the current state, written as iteration `iteration` with
+ * time step dt (the JSON's "time" is iteration * dt). */
+nw_status nw_writer_frame(nw_writer* w, int iteration, float dt);
+/* Wait until every enqueued frame is in the file; reports a write failure. */
+nw_status nw_writer_flush(nw_writer* w);
+nw_status nw_writer_close(nw_writer* w);
 
 /* Numerics self-check of the refined reciprocal, square root and quotient
  * the force laws use (no reference counterpart).  For host arrays a[n] and

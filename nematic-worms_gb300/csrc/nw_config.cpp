@@ -182,6 +182,7 @@ const char* nw_status_string(nw_status s)
     case NW_ERR_NOMEM: return "out of memory";
     case NW_ERR_UNSUPPORTED: return "unsupported configuration";
     case NW_ERR_NO_DEVICE: return "no CUDA device";
+    case NW_ERR_IO: return "file could not be opened or written";
     default: return "unknown status";
     }
 }

@@ -7,6 +7,7 @@
 
 #include "nw_engine.h"
 #include "nw_fused.cuh"
+#include "nw_system.h"
 
 namespace nw {
 
@@ -203,38 +204,6 @@ __global__ void __launch_bounds__(256) ref_hash_kernel(const DevParams P, const 
 }  // namespace nw
 
 using namespace nw;
-
-struct GraphEntry {
-    int nsteps;
-    uint32_t dt_bits;
-    uint32_t phase;
-    uint64_t version;
-    cudaGraphExec_t exec;
-    uint64_t launches;
-};
-
-struct nw_system {
-    NwConfig cfg;
-    int device = 0;
-    cudaStream_t own_stream = nullptr;
-    cudaStream_t stream = nullptr;
-    StepBuffers B;
-    bool lists = false;  // NW_STRATEGY_CELL_LISTS
-    uint32_t nb = 0, ns = 0, ntotal = 0, ncells = 0, nchunks = 0, srd_ncells = 0, srd_nchunks = 0;
-    uint32_t lncells = 0;  // cells of the per-step bead lists (>= the reference grid's when Verlet cells are finer)
-    uint64_t step = 0;
-    uint64_t version = 1;
-    bool use_graphs = true;
-    bool lists_dirty = false;  // list counters must be cleared before the next update
-    uint64_t sorted_for = ~0ull;  // step whose sorted order / cell bounds are in the sort buffers
-    uint32_t scur = 0;            // solvent buffer holding the current solvent (mirror of *B.scur)
-    bool vl = false;              // NW_STRATEGY_VERLET: hash2 holds Verlet-grid hashes
-    bool vl_dirty = true;         // Verlet lists must be rebuilt at the next update
-    uint64_t hash_for = ~0ull;    // step whose reference hashes are in hash2[cur] (Verlet systems)
-    std::vector<GraphEntry> graphs;
-    uint64_t last_launches = 0;
-    std::vector<void*> allocs;
-};
 
 namespace {
 

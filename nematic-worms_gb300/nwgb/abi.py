@@ -27,6 +27,7 @@ NW_ERR_TIMEOUT = 5
 NW_ERR_NOMEM = 6
 NW_ERR_UNSUPPORTED = 7
 NW_ERR_NO_DEVICE = 8
+NW_ERR_IO = 9
 
 NW_EFLAG_NONFINITE = 1 << 0
 NW_EFLAG_CELL_OVERFLOW = 1 << 1
@@ -165,6 +166,7 @@ STATUS_NAMES = {
     NW_ERR_NOMEM: "out of memory",
     NW_ERR_UNSUPPORTED: "unsupported configuration",
     NW_ERR_NO_DEVICE: "no CUDA device",
+    NW_ERR_IO: "file could not be opened or written",
 }
 
 # Every symbol the library must export: (name, restype, argtypes)
@@ -200,6 +202,10 @@ HANDLE_API = [
     ("nw_last_launch_count", C.c_int, [_sysp, C.POINTER(C.c_uint64)]),
     ("nw_profile_steps", C.c_int, [_sysp, C.c_int, _f32, C.POINTER(NwKernelTime), C.c_int, C.POINTER(C.c_int)]),
     ("nw_math_probe", C.c_int, [C.c_void_p, C.c_void_p, _u32, C.c_void_p]),
+    ("nw_writer_open", C.c_int, [_sysp, C.c_char_p, C.c_int, C.POINTER(_P)]),
+    ("nw_writer_frame", C.c_int, [_P, C.c_int, _f32]),
+    ("nw_writer_flush", C.c_int, [_P]),
+    ("nw_writer_close", C.c_int, [_P]),
 ]
 
 _fp = C.c_void_p  # device pointers are passed as integers

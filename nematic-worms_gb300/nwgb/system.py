@@ -43,6 +43,12 @@ class System:
     def __enter__(self):
         return self
 
+    def writer(self, path, append: bool = False):
+        """Trajectory writer of this system (nwgb.trajectory.Writer)."""
+        from .trajectory import Writer
+
+        return Writer(self, path, append)
+
     def __exit__(self, *exc):
         self.close()
 
