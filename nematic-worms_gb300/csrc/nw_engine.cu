@@ -179,8 +179,10 @@ uint64_t enqueue_srd(const DevParams& P, const StepBuffers& B, uint32_t srd_nchu
     srd_scatter_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(P, B);
     NW_MARK("srd_collide");
     srd_collide_kernel<<<cdiv(P.srd_ncells, 256), 256, 0, s>>>(P, B, step_off, dt_srd, buf_sel);
+    NW_MARK("srd_collide_big");
+    srd_collide_big_kernel<<<kSrdBigBlocks, 256, 0, s>>>(P, B, step_off, dt_srd, buf_sel);
     srd_flip_kernel<<<1, 1, 0, s>>>(B.scur);
-    return 8;
+    return 9;
 }
 
 // Histogram of bead hashes (the counting sort's first pass, for the sorted
@@ -549,6 +551,8 @@ nw_status nw_create(const NwConfig* cfg, nw_system** out)
         A(alloc_n(s, &B.srd_bchunk, (size_t)s->srd_nchunks + 1));
         A(alloc_n(s, &B.srd_schunk, (size_t)s->srd_nchunks + 1));
         A(alloc_n(s, &B.srd_mean, Cs));
+        A(alloc_n(s, &B.srd_big, Cs + 8));
+        A(alloc_n(s, &B.srd_nbig, 4));
     }
     A(alloc_n(s, &B.err, 4));
     A(alloc_n(s, &B.step_base, 1));

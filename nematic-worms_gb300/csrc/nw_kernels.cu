@@ -272,6 +272,7 @@ __global__ void __launch_bounds__(256) srd_scatter_kernel(const DevParams P, con
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.ntotal) return;
+    if (i == 0) *S.srd_nbig = 0;  // the list is filled by the collision that follows
     const uint32_t h = S.srd_hash[i], slot = S.srd_slot[i];
     if (i < P.nb) S.srd_btmp[S.srd_boff[h] + slot] = i;
     else S.srd_stmp[S.srd_soff[h] + slot] = i - P.nb;
@@ -290,8 +291,10 @@ __global__ void __launch_bounds__(256) srd_scatter_kernel(const DevParams P, con
 // ([slot][thread], conflict-free) and keeps the first kSrdVel member
 // velocities there too, so every velocity is gathered from global memory
 // once; positions are gathered once, in the final pass.  Cells with more
-// than kSrdIds members (a Poisson tail at the usual densities) rank their
-// members in global memory instead.
+// than kSrdIds members (a Poisson tail at rest; a few percent once active
+// flows compress the solvent) go to srd_collide_big_kernel, a warp per
+// cell; cells beyond kStableCap are flagged and ranked in global memory
+// with bounded work.
 constexpr int kSrdThreads = 256;
 constexpr uint32_t kSrdIds = 16;
 constexpr uint32_t kSrdVel = 8;
@@ -320,6 +323,10 @@ __global__ void __launch_bounds__(kSrdThreads) srd_collide_kernel(const DevParam
     S.srd_end[c] = n ? start + n : kEmpty;
     float3 u = zero3();
     if (n > 0) {
+        if (n > kSrdIds && n <= kStableCap) {
+            S.srd_big[atomicAdd(S.srd_nbig, 1u)] = c;
+            return;
+        }
         // members in stable order: ids < nb are beads, nb + k is solvent k
         const bool local = n <= kSrdIds;
         if (n > kStableCap) atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
@@ -421,6 +428,133 @@ __global__ void __launch_bounds__(kSrdThreads) srd_collide_kernel(const DevParam
         }
     }
     S.srd_mean[c] = make_float4(u.x, u.y, u.z, 0.f);
+}
+
+__device__ __forceinline__ float warp_allsum(float x)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+
+// The collision of srd_collide_kernel for one cell of kSrdIds < n <=
+// kStableCap members, by one warp: members ranked by index in shared memory
+// (the stable order), their velocities gathered once into shared memory,
+// sums as lane-strided partials combined by a fixed butterfly (the same
+// result on every run), then the per-member update by all lanes.
+constexpr uint32_t kBigWarps = 8;
+__global__ void __launch_bounds__(256) srd_collide_big_kernel(const DevParams P, const StepBuffers S,
+                                                              uint32_t step_off, float dt_srd, uint32_t buf_sel)
+{
+    __shared__ uint32_t s_in[kBigWarps][kStableCap];
+    __shared__ uint32_t s_id[kBigWarps][kStableCap];
+    __shared__ float4 s_v[kBigWarps][kStableCap];
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    const uint32_t nbig = *S.srd_nbig;
+    const unsigned long long step = *S.step_base + step_off;
+    const uint32_t cur = buf_sel < 2u ? buf_sel : (uint32_t)(step & 1ull);
+    const uint32_t a = *S.scur;
+    const float4* __restrict__ sv_old = S.svel2[a];
+    const float4* __restrict__ sp_old = S.spos2[a];
+    float4* __restrict__ sv_new = S.svel2[a ^ 1u];
+    float4* __restrict__ sp_new = S.spos2[a ^ 1u];
+    float4* __restrict__ bvel = S.vel2[cur];
+    const bool lab = P.srd_thermo == NW_SRD_THERMO_REF_LAB;
+    const bool rel = P.srd_thermo == NW_SRD_THERMO_CELL_REL;
+    for (uint32_t q = blockIdx.x * kBigWarps + w; q < nbig; q += gridDim.x * kBigWarps) {
+        const uint32_t c = S.srd_big[q];
+        const uint32_t b0 = S.srd_boff[c], b1 = S.srd_boff[c + 1];
+        const uint32_t s0 = S.srd_soff[c], s1 = S.srd_soff[c + 1];
+        const uint32_t nbc = b1 - b0, n = nbc + (s1 - s0);
+        const uint32_t start = b0 + s0;
+        for (uint32_t k = lane; k < n; k += 32)
+            s_in[w][k] = k < nbc ? S.srd_btmp[b0 + k] : P.nb + S.srd_stmp[s0 + (k - nbc)];
+        __syncwarp();
+        for (uint32_t k = lane; k < n; k += 32) {
+            const uint32_t x = s_in[w][k];
+            uint32_t r = 0;
+            for (uint32_t j = 0; j < n; ++j) r += s_in[w][j] < x;
+            s_id[w][r] = x;
+        }
+        __syncwarp();
+        float E = 0.f;
+        for (uint32_t k = lane; k < n; k += 32) {
+            const uint32_t id = s_id[w][k];
+            S.srd_sorted_index[start + k] = id;
+            const float4 V = id < P.nb ? bvel[id] : sv_old[id - P.nb];
+            s_v[w][k] = V;
+            E += (0.5f * V.w) * (V.x * V.x + V.y * V.y + V.z * V.z);
+        }
+        __syncwarp();
+        E = warp_allsum(E);
+        const float lam1 = lab ? sqrtf(P.srd_kT / E) : 1.0f;
+        float ux = 0.f, uy = 0.f, uz = 0.f, M = 0.f;
+        for (uint32_t k = lane; k < n; k += 32) {
+            const float4 V = s_v[w][k];
+            const float sx = lab ? lam1 * V.x : V.x, sy = lab ? lam1 * V.y : V.y, sz = lab ? lam1 * V.z : V.z;
+            ux += V.w * sx;
+            uy += V.w * sy;
+            uz += V.w * sz;
+            M += V.w;
+        }
+        ux = warp_allsum(ux);
+        uy = warp_allsum(uy);
+        uz = warp_allsum(uz);
+        M = warp_allsum(M);
+        if (M > 0.f) {
+            const float inv = 1.0f / M;
+            ux *= inv;
+            uy *= inv;
+            uz *= inv;
+        }
+        const bool plus = u01(rng_draw(P, c, step, kRngSrdRot).x) > 0.5f;
+        const float sa = plus ? P.srd_sin_a : -P.srd_sin_a, ca = P.srd_cos_a;
+        float lam2 = 1.0f;
+        bool scale2 = false;
+        if (rel) {
+            float ke = 0.f, nrot = 0.f;
+            for (uint32_t k = lane; k < n; k += 32) {
+                if (s_id[w][k] < P.nb && !P.srd_rotate_beads) continue;
+                const float4 V = s_v[w][k];
+                const float dx = (lab ? lam1 * V.x : V.x) - ux, dy = (lab ? lam1 * V.y : V.y) - uy;
+                const float rx = dx * ca - dy * sa, ry = dx * sa + dy * ca;
+                ke += (0.5f * V.w) * (rx * rx + ry * ry);
+                nrot += 1.f;
+            }
+            ke = warp_allsum(ke);
+            nrot = warp_allsum(nrot);
+            if (nrot >= 2.f && ke > 0.f) {
+                lam2 = sqrtf(((nrot - 1.f) * P.srd_kT) / ke);
+                scale2 = true;
+            }
+        }
+        for (uint32_t k = lane; k < n; k += 32) {
+            const uint32_t id = s_id[w][k];
+            const bool is_bead = id < P.nb;
+            const float4 V = s_v[w][k];
+            float3 v = lab ? make_float3(lam1 * V.x, lam1 * V.y, lam1 * V.z) : f3(V);
+            if (!is_bead || P.srd_rotate_beads) {
+                const float dx = v.x - ux, dy = v.y - uy, dz = v.z - uz;
+                const float rx = dx * ca - dy * sa, ry = dx * sa + dy * ca;
+                v = make_float3(ux + rx, uy + ry, uz + dz);
+                if (scale2) v = make_float3(ux + lam2 * (v.x - ux), uy + lam2 * (v.y - uy), v.z);
+            }
+            if (is_bead) {
+                if (lab || P.srd_rotate_beads) bvel[id] = make_float4(v.x, v.y, v.z, V.w);
+            } else {
+                const float4 P4 = sp_old[id - P.nb];
+                float3 p = f3(P4);
+                const float3 dr = dt_srd * v;
+                p += dr;
+                apply_boundaries(P, p, v, dr, 0.0f);
+                const uint32_t dst = s0 + (k - nbc);
+                sp_new[dst] = make_float4(p.x, p.y, p.z, P4.w);
+                sv_new[dst] = make_float4(v.x, v.y, v.z, V.w);
+            }
+        }
+        if (lane == 0) S.srd_mean[c] = make_float4(ux, uy, uz, 0.f);
+        __syncwarp();
+    }
 }
 
 // The collision just written the solvent to the other buffer.

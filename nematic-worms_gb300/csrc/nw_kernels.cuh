@@ -1,14 +1,18 @@
 // nw_kernels.cuh — the step kernels of the GB300 worm engine.
 //
-// One step is five launches (plus four every srd_gap steps):
+// Sorted strategy (the reference's scheme), six launches per step:
 //   filament_pass   integrate + [reverse] + Langevin + bending/tangents
 //                   [+ bonds + drive] + cell hash + counting-sort slot
+//   chunk_sum       totals of 4096-cell chunks of the cell counts
 //   scan_cells      cell offsets / starts / ends from the cell counts
 //   scatter         bucket the bead indices by cell
 //   stable_gather   order every bucket by index (the stable sort) and
 //                   gather positions (+ velocities and tangents) in cell order
 //   pair_*          pair forces over the 3x3(x3) neighbour cells
-//   [srd_hash, scan_cells, scatter, srd_collide]
+// The cell-list and Verlet strategies (nw_fused.cu) run one fused kernel
+// per step instead.  Every srd_gap steps an SRD collision adds nine:
+//   srd_hash, chunk_sum x2, scan_cells x2 (bead and solvent buckets),
+//   srd_scatter, srd_collide, srd_collide_big, srd_flip.
 //
 // No float atomics are used anywhere: every output element has exactly one
 // writer, so repeated runs are bit-identical.
@@ -54,6 +58,9 @@ struct StepBuffers {
     uint32_t *srd_bcount, *srd_scount, *srd_boff, *srd_soff, *srd_bchunk, *srd_schunk;
     uint32_t *srd_start, *srd_end;
     float4* srd_mean;
+    // SRD cells too full for one thread (kSrdIds < members <= kStableCap),
+    // handed to srd_collide_big_kernel: srd_big[0 .. *srd_nbig)
+    uint32_t *srd_big, *srd_nbig;
     uint32_t* err;
     unsigned long long* step_base;
 };
@@ -531,6 +538,10 @@ __global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, con
                                                           float dt_srd, uint32_t buf_sel);
 
 __global__ void __launch_bounds__(256) srd_scatter_kernel(const DevParams P, const StepBuffers S);
+// One warp per SRD cell of the srd_big list (grid-stride over the list).
+__global__ void __launch_bounds__(256) srd_collide_big_kernel(const DevParams P, const StepBuffers S,
+                                                              uint32_t step_off, float dt_srd, uint32_t buf_sel);
+constexpr uint32_t kSrdBigBlocks = 608;  // 4 blocks of 8 warps per SM
 __global__ void srd_flip_kernel(uint32_t* scur);
 
 __global__ void advance_step_kernel(unsigned long long* step_base, unsigned long long k);

@@ -32,6 +32,11 @@ def make_case(kind: str, lib):
         cfg = wca_config(80, 10, (40.0, 40.0), srd=True, seed=2, lib=lib)
         pos, vel = initial_state(cfg, seed=2)
         tan = np.zeros((cfg.n_beads, 4), np.float32)
+    elif kind == "wca_srd_dense":
+        # 24 solvent per SRD cell: most cells take the warp-per-cell collision
+        cfg = wca_config(80, 10, (40.0, 40.0), srd=True, srd_density=24.0, seed=6, lib=lib)
+        pos, vel = initial_state(cfg, seed=6)
+        tan = np.zeros((cfg.n_beads, 4), np.float32)
     elif kind == "wca_reverse":
         cfg = wca_config(60, 12, (40.0, 40.0), seed=3, lib=lib)
         cfg.reverse_probability = 0.4
@@ -87,10 +92,10 @@ def run_oracle(orc, cfg, pos, vel, tan, nsteps=1, prec=32):
     return st
 
 
-CASES = ["wca", "wca_srd", "wca_reverse", "ref", "ref_srd", "ref_walls"]
+CASES = ["wca", "wca_srd", "wca_srd_dense", "wca_reverse", "ref", "ref_srd", "ref_walls"]
 STRATEGIES = [abi.NW_STRATEGY_CELL_LISTS, abi.NW_STRATEGY_SORTED, abi.NW_STRATEGY_VERLET]
 # launches of one update: (bead step, SRD collision) + the step counter
-LAUNCHES = {abi.NW_STRATEGY_CELL_LISTS: (2, 8), abi.NW_STRATEGY_SORTED: (6, 8), abi.NW_STRATEGY_VERLET: (2, 8)}
+LAUNCHES = {abi.NW_STRATEGY_CELL_LISTS: (2, 9), abi.NW_STRATEGY_SORTED: (6, 9), abi.NW_STRATEGY_VERLET: (2, 9)}
 
 
 def strategy_applies(kind, strategy):
@@ -130,7 +135,7 @@ def test_one_step_matches_oracle(lib, orc, kind, strategy):
 
 
 @pytest.mark.parametrize("strategy", STRATEGIES)
-@pytest.mark.parametrize("kind", ["wca", "ref_srd"])
+@pytest.mark.parametrize("kind", ["wca", "ref_srd", "wca_srd_dense"])
 def test_graph_replay_is_bit_identical_to_direct_launches(lib, kind, strategy):
     if not strategy_applies(kind, strategy):
         pytest.skip("Verlet lists are WCA-only")
