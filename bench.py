@@ -566,7 +566,10 @@ def run_adjoint(args):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20000)
+    # the workload is defined as a 10,000-step run: the active drive pumps
+    # momentum into the solvent (no Langevin friction with SRD), so the state
+    # keeps warming and longer runs measure a different, hotter system
+    ap.add_argument("--steps", type=int, default=10000)
     ap.add_argument("--warmup", type=int, default=100)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="wca_srd_400k")
