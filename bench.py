@@ -53,42 +53,52 @@ def env_rank():
 
 
 # ---- algorithmic bytes per launch (reference float4 state model) -------------------
+# Units of work and their compulsory bytes in the reference's float4 layout:
+#   bead-step:  96 B (pos, vel, force read and written: 3 x 16 B each way)
+#               + 16 B (one write and one read of the 8 B (key, value) pair)
+#               + 8 C / N B (cell start/end written once and read once)
+#   SRD collision, per solvent particle: 64 B (pos and vel read and written)
+#               + 16 B (key, value) + 32 Cs / Ns B (cell momentum and energy sums)
+BEAD_STEP_B = 112.0
+SRD_PARTICLE_B = 80.0
+
+
+def step_bytes(cfg) -> float:
+    """Algorithmic bytes of one step: every bead-step plus the SRD collision
+    amortised over its period."""
+    b = cfg.n_beads * BEAD_STEP_B + 8.0 * cfg.n_cells
+    if cfg.srd_enabled:
+        b += (cfg.n_solvent * SRD_PARTICLE_B + 32.0 * cfg.n_srd_cells) / max(1, int(cfg.srd_gap))
+    return b
+
+
 def alg_bytes(name: str, cfg) -> float:
-    """Compulsory DRAM bytes of one launch of kernel `name`: every input read
-    once, every output written once, in the reference's float4 layout."""
-    nb, nt = cfg.n_beads, cfg.n_beads + cfg.n_solvent
+    """Compulsory DRAM bytes of one launch of kernel `name` in the units
+    above: a kernel that completes a bead-step for every bead (the fused
+    step kernel; the pair kernel of the sorted scheme, which finishes it)
+    carries 112 N + 8 C; the collision kernel carries the collision's
+    80 Ns + 32 Cs.  Kernels that only prepare a unit carry their own reads
+    and writes (the sort's passes: 16 N over the pass, cell tables 8 C)."""
+    nb, ns = cfg.n_beads, cfg.n_solvent
     C, Cs = cfg.n_cells, cfg.n_srd_cells
-    ns = cfg.n_solvent
+    step = 112.0 * nb + 8.0 * C
     table = {
-        # r, v, f, f_old read (64 B); r, v, f_old, f, tangent written (80 B); hash + slot (8 B)
-        "filament_pass": 152.0 * nb,
-        # count read, offset/start/end written, count reset
-        "scan_cells": 20.0 * C,
-        # bead and solvent bucket counts read, offsets written, counts reset
-        "srd_scan_cells": 24.0 * Cs,
-        "srd_chunk_sum": 8.0 * Cs,
+        "bead_fused": step,
+        "bead_epi": step,  # the pair pass that completes the step before a collision
+        "pair_wca": step,
+        "pair_ref": step,
+        "srd_collide": SRD_PARTICLE_B * ns + 32.0 * Cs,
+        # preparation passes: their own compulsory traffic
+        "bead_pro": 64.0 * nb + 16.0 * nb,
+        "filament_pass": 64.0 * nb + 16.0 * nb,
+        "scan_cells": 8.0 * C,
         "chunk_sum": 4.0 * C,
-        # hash + slot read, index written
-        "scatter": 12.0 * nb,
-        # hash + slot read, bucket offset read, bucket entry written
-        "srd_scatter": 16.0 * nt,
-        # bucket index + hash + position read; sorted index, hash, position written
-        "stable_gather": 48.0 * nb,
-        # sorted position + index read, force read-modify-write, cell bounds read
-        "pair_wca": 52.0 * nb + 8.0 * C,
-        "pair_ref": 84.0 * nb + 8.0 * C,
-        # cell-list path: pro = integrate .. hash + list insert (r, v, f, f_old in; r, v, f_old, f,
-        # tangent, hash, list slot out; list count update and clearing per cell)
-        "bead_pro": 156.0 * nb + 8.0 * C,
-        # epi: own position, force read-modify-write, list counts
-        "bead_epi": 48.0 * nb + 4.0 * C,
-        # fused = epi(n) + pro(n+1) with the complete force kept in a register
-        "bead_fused": 156.0 * nb + 12.0 * C,
-        # position read, hash + slot written
-        "srd_hash": 24.0 * nt,
-        # bucket entry + velocity read, stable index written; bead velocity written in place;
-        # solvent position read, position + velocity written in cell order; offsets, bounds, mean
-        "srd_collide": 24.0 * nt + 16.0 * nb + 48.0 * ns + 32.0 * Cs,
+        "scatter": 16.0 * nb,
+        "stable_gather": 16.0 * nb,
+        "srd_hash": 16.0 * (nb + ns) + 8.0 * (nb + ns),
+        "srd_scatter": 16.0 * (nb + ns),
+        "srd_scan_cells": 16.0 * Cs,
+        "srd_chunk_sum": 8.0 * Cs,
         "advance_step": 8.0,
     }
     return table.get(name, 0.0)
@@ -360,9 +370,13 @@ def run_ours(args):
         units = {"bead": nb, "particle": nb + cfg.n_solvent, "cell": cfg.n_cells, "srd_cell": cfg.n_srd_cells}.get(unit)
         traffic = per_unit * units if units else None
     total_prof = sum(v[0] for v in prof.values())
+    sb = step_bytes(cfg)
+    step_gbs = sb / (ms_max / args.steps / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
                 "traffic": traffic, "alg_bytes_per_launch": bytes_launch, "avg_launch_ms": dom_ms,
+                "step": {"alg_bytes": sb, "achieved": step_gbs, "frac": step_gbs / peak,
+                         "note": "whole step (timed value) against the same peak"},
                 "kernel_share": {k: round(v[0] / total_prof, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}}
 
     if rank == 0:
