@@ -10,6 +10,8 @@ sets the force scale).
 """
 from __future__ import annotations
 
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -59,9 +61,51 @@ def make_case(kind: str, lib):
         pos, vel, tan = reference_reset(cfg)
         rng = np.random.default_rng(4)
         pos[:cfg.n_beads, :2] += rng.normal(0, 0.05, (cfg.n_beads, 2)).astype(np.float32)
+    elif kind in ("wca_3d", "ref_3d"):
+        # 3D grids: straight worms along x on a jittered y-z lattice of rows
+        if kind == "wca_3d":
+            cfg = abi.default_config(abi.NW_MODEL_WCA_WORMS, 96, 10, (18, 12, 12), False, lib)
+            cfg.dim = 3
+            for a in range(3):
+                cfg.cell_size[a] = 1.125
+            abi.check(lib.nw_config_finalize(C.byref(cfg)))
+            cfg.seed = 12
+        else:
+            cfg = abi.default_config(abi.NW_MODEL_REF_DEM, 96, 10, (32, 16, 16), False, lib)
+            cfg.bond_r0 = 0.8
+            cfg.activity = 0.5
+            cfg.kT = 0.1
+            cfg.seed = 13
+        pos, vel, tan = lattice_3d(cfg, seed=7)
     else:
         raise ValueError(kind)
     return cfg, pos, vel, tan
+
+
+def lattice_3d(cfg, seed):
+    """Worms along x in rows on a y-z lattice (pitch 1.5), jittered; Maxwell-
+    Boltzmann velocities in three dimensions."""
+    rng = np.random.default_rng(seed)
+    M, L = cfg.num_filaments, cfg.filament_size
+    org = np.array([cfg.origin[0], cfg.origin[1], cfg.origin[2]])
+    box = np.array([cfg.box[0], cfg.box[1], cfg.box[2]])
+    length = (L - 1) * cfg.bond_r0
+    per_x = int(box[0] // (length + 1.0))
+    ny, nz = int(box[1] // 1.5), int(box[2] // 1.5)
+    assert per_x * ny * nz >= M
+    pos = np.zeros((M * L, 4), np.float32)
+    for w in range(M):
+        ix, rest = w % per_x, w // per_x
+        iy, iz = rest % ny, rest // ny
+        head = org + np.array([ix * (length + 1.0) + 0.5, (iy + 0.5) * 1.5, (iz + 0.5) * 1.5])
+        head[1:] += rng.normal(0, 0.05, 2)
+        beads = head[None, :] + np.arange(L)[:, None] * np.array([cfg.bond_r0, 0.0, 0.0])[None, :]
+        pos[w * L:(w + 1) * L, :3] = beads
+    pos[:, 3] = cfg.radius
+    vel = np.zeros_like(pos)
+    vel[:, :3] = rng.normal(0, np.sqrt(cfg.kT), (M * L, 3))
+    vel[:, 3] = cfg.mass
+    return pos, vel, np.zeros_like(pos)
 
 
 def run_gpu(cfg, pos, vel, tan, nsteps=1, graphs=True):
@@ -92,7 +136,7 @@ def run_oracle(orc, cfg, pos, vel, tan, nsteps=1, prec=32):
     return st
 
 
-CASES = ["wca", "wca_srd", "wca_srd_dense", "wca_reverse", "ref", "ref_srd", "ref_walls"]
+CASES = ["wca", "wca_srd", "wca_srd_dense", "wca_reverse", "wca_3d", "ref", "ref_srd", "ref_walls", "ref_3d"]
 STRATEGIES = [abi.NW_STRATEGY_CELL_LISTS, abi.NW_STRATEGY_SORTED, abi.NW_STRATEGY_VERLET]
 # launches of one update: (bead step, SRD collision) + the step counter
 LAUNCHES = {abi.NW_STRATEGY_CELL_LISTS: (2, 9), abi.NW_STRATEGY_SORTED: (6, 9), abi.NW_STRATEGY_VERLET: (2, 9)}
