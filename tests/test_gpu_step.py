@@ -72,11 +72,17 @@ def make_case(kind: str, lib):
             cfg.seed = 12
         else:
             cfg = abi.default_config(abi.NW_MODEL_REF_DEM, 96, 10, (32, 16, 16), False, lib)
+            # the parameters of the 2D REF_DEM cases
             cfg.bond_r0 = 0.8
+            cfg.bend_k = 10.0
             cfg.activity = 0.5
+            cfg.spring = 57.0
             cfg.kT = 0.1
+            cfg.gamma = 2.0
             cfg.seed = 13
         pos, vel, tan = lattice_3d(cfg, seed=7)
+        # off the relaxed lattice, as the 2D REF_DEM cases are
+        pos[:, :3] += np.random.default_rng(8).normal(0, 0.05, (cfg.n_beads, 3)).astype(np.float32)
     else:
         raise ValueError(kind)
     return cfg, pos, vel, tan
