@@ -481,7 +481,7 @@ __global__ void __launch_bounds__(256) bead_epi_kernel(const DevParams P, const 
 
 // epi(n) then pro(n+1): the complete force of update n stays in a register.
 template <int CAP, bool kRef, int MAXT>
-__global__ void __launch_bounds__(MAXT) bead_fused_kernel(const DevParams P, const StepBuffers S, uint32_t off,
+__global__ void __launch_bounds__(MAXT, (MAXT == 256 && !kRef) ? 6 : 1) bead_fused_kernel(const DevParams P, const StepBuffers S, uint32_t off,
                                                           float dt, uint32_t fpb)
 {
     const unsigned long long n = *S.step_base + off;
