@@ -178,7 +178,7 @@ uint64_t enqueue_srd(const DevParams& P, const StepBuffers& B, uint32_t srd_nchu
     NW_MARK("srd_scatter");
     srd_scatter_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(P, B);
     NW_MARK("srd_collide");
-    srd_collide_kernel<<<cdiv(P.srd_ncells, 256), 256, 0, s>>>(P, B, step_off, dt_srd, buf_sel);
+    srd_collide_kernel<<<cdiv(P.srd_ncells, 128), 128, 0, s>>>(P, B, step_off, dt_srd, buf_sel);
     NW_MARK("srd_collide_big");
     srd_collide_big_kernel<<<kSrdBigBlocks, 256, 0, s>>>(P, B, step_off, dt_srd, buf_sel);
     srd_flip_kernel<<<1, 1, 0, s>>>(B.scur);

@@ -278,35 +278,35 @@ __global__ void __launch_bounds__(256) srd_scatter_kernel(const DevParams P, con
     else S.srd_stmp[S.srd_soff[h] + slot] = i - P.nb;
 }
 
-// One SRD cell per thread.  Members in the stable (cell, index) order: the
-// cell's beads, then its solvent.  The reference's isokinetic scaling
-// (particles_kernel_impl.cuh:605-637) or none, the mass-weighted cell mean
-// (:560-594), the +/- alpha rotation of (v - u) (:640-691), the
-// relative-velocity thermostat when selected, and the solvent's ballistic
-// streaming by dt_srd (solvent_integrator, :145-205).  Beads are written in
-// place, the solvent to the other solvent buffer at its new position in
-// cell order.
+// SRD collision.  A warp owns 32 consecutive cells; their members are one
+// contiguous range of the stable (cell, index) order and their solvent one
+// contiguous range of the new solvent storage.  So the warp gathers the
+// members' velocities and positions lane-strided into shared memory (the
+// previous collision's cell order keeps them in a compact region), each
+// thread collides its own cell from shared memory, and the warp writes the
+// stable order and the streamed solvent back coalesced.
 //
-// Memory: each thread sorts its member ids in its own shared-memory column
-// ([slot][thread], conflict-free) and keeps the first kSrdVel member
-// velocities there too, so every velocity is gathered from global memory
-// once; positions are gathered once, in the final pass.  Cells with more
-// than kSrdIds members (a Poisson tail at rest; a few percent once active
-// flows compress the solvent) go to srd_collide_big_kernel, a warp per
-// cell; cells beyond kStableCap are flagged and ranked in global memory
-// with bounded work.
-constexpr int kSrdThreads = 256;
-constexpr uint32_t kSrdIds = 16;
-constexpr uint32_t kSrdVel = 8;
+// Per cell, in the member order (the cell's beads, then its solvent, each by
+// index): the reference's isokinetic scaling (particles_kernel_impl.cuh:605-637)
+// or none, the mass-weighted cell mean (:560-594), the +/- alpha rotation of
+// (v - u) (:640-691), the relative-velocity thermostat when selected, and the
+// solvent's ballistic streaming by dt_srd (solvent_integrator, :145-205).
+// Beads are written in place, the solvent to the other solvent buffer.
+// Warps holding more than kWarpCap members hand their cells to
+// srd_collide_big_kernel (a warp per cell).
+constexpr int kCollideWarps = 4;
+constexpr uint32_t kWarpCap = 256;
 
-__global__ void __launch_bounds__(kSrdThreads) srd_collide_kernel(const DevParams P, const StepBuffers S,
-                                                                  uint32_t step_off, float dt_srd, uint32_t buf_sel)
+__global__ void __launch_bounds__(kCollideWarps * 32) srd_collide_kernel(const DevParams P, const StepBuffers S,
+                                                                         uint32_t step_off, float dt_srd,
+                                                                         uint32_t buf_sel)
 {
-    __shared__ uint32_t s_ids[kSrdIds][kSrdThreads];
-    __shared__ float4 s_vel[kSrdVel][kSrdThreads];
-    const uint32_t t = threadIdx.x;
-    const uint32_t c = blockIdx.x * blockDim.x + t;
-    if (c >= P.srd_ncells) return;
+    __shared__ uint32_t s_id[kCollideWarps][kWarpCap];
+    __shared__ float4 s_v[kCollideWarps][kWarpCap];
+    __shared__ float4 s_p[kCollideWarps][kWarpCap];
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = c < P.srd_ncells;
     const unsigned long long step = *S.step_base + step_off;
     const uint32_t cur = buf_sel < 2u ? buf_sel : (uint32_t)(step & 1ull);
     const uint32_t a = *S.scur;
@@ -315,53 +315,59 @@ __global__ void __launch_bounds__(kSrdThreads) srd_collide_kernel(const DevParam
     float4* __restrict__ sv_new = S.svel2[a ^ 1u];
     float4* __restrict__ sp_new = S.spos2[a ^ 1u];
     float4* __restrict__ bvel = S.vel2[cur];
-    const uint32_t b0 = S.srd_boff[c], b1 = S.srd_boff[c + 1];
-    const uint32_t s0 = S.srd_soff[c], s1 = S.srd_soff[c + 1];
-    const uint32_t nbc = b1 - b0, nsc = s1 - s0, n = nbc + nsc;
+    uint32_t b0 = 0, nbc = 0, s0 = 0, nsc = 0;
+    if (valid) {
+        b0 = S.srd_boff[c];
+        nbc = S.srd_boff[c + 1] - b0;
+        s0 = S.srd_soff[c];
+        nsc = S.srd_soff[c + 1] - s0;
+    }
+    const uint32_t n = nbc + nsc;
     const uint32_t start = b0 + s0;  // particles before this cell in the stable order
-    S.srd_start[c] = n ? start : kEmpty;
-    S.srd_end[c] = n ? start + n : kEmpty;
+    if (valid) {
+        S.srd_start[c] = n ? start : kEmpty;
+        S.srd_end[c] = n ? start + n : kEmpty;
+    }
+    const uint32_t incl = warp_incl_scan(n);
+    const uint32_t loc = incl - n;  // this cell's members in the warp's range
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0u || total > kWarpCap) {  // uniform over the warp
+        if (valid && n > 0u) S.srd_big[atomicAdd(S.srd_nbig, 1u)] = c;
+        else if (valid) S.srd_mean[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    // members of this cell in stable order: ids < nb are beads, nb + k is solvent k
+    uint32_t* ids = &s_id[w][loc];
+    for (uint32_t k = 0; k < n; ++k) {
+        const uint32_t x = k < nbc ? S.srd_btmp[b0 + k] : P.nb + S.srd_stmp[s0 + (k - nbc)];
+        uint32_t m = k;
+        while (m > 0 && ids[m - 1] > x) {
+            ids[m] = ids[m - 1];
+            --m;
+        }
+        ids[m] = x;
+    }
+    __syncwarp();
+    const uint32_t wstart = __shfl_sync(0xffffffffu, start, 0);
+    for (uint32_t k = lane; k < total; k += 32) {
+        const uint32_t id = s_id[w][k];
+        S.srd_sorted_index[wstart + k] = id;
+        if (id < P.nb) {
+            s_v[w][k] = bvel[id];
+        } else {
+            s_v[w][k] = sv_old[id - P.nb];
+            s_p[w][k] = sp_old[id - P.nb];
+        }
+    }
+    __syncwarp();
     float3 u = zero3();
     if (n > 0) {
-        if (n > kSrdIds && n <= kStableCap) {
-            S.srd_big[atomicAdd(S.srd_nbig, 1u)] = c;
-            return;
-        }
-        // members in stable order: ids < nb are beads, nb + k is solvent k
-        const bool local = n <= kSrdIds;
-        if (n > kStableCap) atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
-        if (local) {
-            for (uint32_t k = 0; k < n; ++k) {
-                const uint32_t x = k < nbc ? S.srd_btmp[b0 + k] : P.nb + S.srd_stmp[s0 + (k - nbc)];
-                uint32_t m = k;
-                while (m > 0 && s_ids[m - 1][t] > x) {
-                    s_ids[m][t] = s_ids[m - 1][t];
-                    --m;
-                }
-                s_ids[m][t] = x;
-            }
-            for (uint32_t k = 0; k < n; ++k) S.srd_sorted_index[start + k] = s_ids[k][t];
-        } else {
-            for (uint32_t q = b0; q < b1; ++q) {
-                const uint32_t x = S.srd_btmp[q];
-                const uint32_t r = nbc <= kStableCap ? bucket_rank(S.srd_btmp, b0, b1, x, q, S.err) : q - b0;
-                S.srd_sorted_index[start + r] = x;
-            }
-            for (uint32_t q = s0; q < s1; ++q) {
-                const uint32_t x = S.srd_stmp[q];
-                const uint32_t r = nsc <= kStableCap ? bucket_rank(S.srd_stmp, s0, s1, x, q, S.err) : q - s0;
-                S.srd_sorted_index[start + nbc + r] = P.nb + x;
-            }
-        }
-        auto member = [&](uint32_t k) -> uint32_t { return local ? s_ids[k][t] : S.srd_sorted_index[start + k]; };
-        auto gather = [&](uint32_t id) -> float4 { return id < P.nb ? bvel[id] : sv_old[id - P.nb]; };
-        // velocity of member k: gathered once, then from the shared-memory cache
-        auto vel_at = [&](uint32_t k) -> float4 { return k < kSrdVel ? s_vel[k][t] : gather(member(k)); };
+        float4* V_ = &s_v[w][loc];
+        float4* P_ = &s_p[w][loc];
         const bool lab = P.srd_thermo == NW_SRD_THERMO_REF_LAB;
         float E = 0.f;
         for (uint32_t k = 0; k < n; ++k) {
-            const float4 V = gather(member(k));
-            if (k < kSrdVel) s_vel[k][t] = V;
+            const float4 V = V_[k];
             const float3 v = f3(V);
             E += (0.5f * V.w) * dot3(v, v);
         }
@@ -370,7 +376,7 @@ __global__ void __launch_bounds__(kSrdThreads) srd_collide_kernel(const DevParam
         auto scaled = [&](float4 V) -> float3 { return lab ? make_float3(lam1 * V.x, lam1 * V.y, lam1 * V.z) : f3(V); };
         float M = 0.f;
         for (uint32_t k = 0; k < n; ++k) {
-            const float4 V = vel_at(k);
+            const float4 V = V_[k];
             u += V.w * scaled(V);
             M += V.w;
         }
@@ -381,15 +387,14 @@ __global__ void __launch_bounds__(kSrdThreads) srd_collide_kernel(const DevParam
         // rotation by +alpha or -alpha with equal probability
         const bool plus = u01(rng_draw(P, c, step, kRngSrdRot).x) > 0.5f;
         const float sa = plus ? P.srd_sin_a : -P.srd_sin_a, ca = P.srd_cos_a;
-        const bool rel = P.srd_thermo == NW_SRD_THERMO_CELL_REL;
         float lam2 = 1.0f;
         bool scale2 = false;
-        if (rel) {
+        if (P.srd_thermo == NW_SRD_THERMO_CELL_REL) {
             uint32_t nrot = 0;
             float ke = 0.f;
             for (uint32_t k = 0; k < n; ++k) {
-                if (member(k) < P.nb && !P.srd_rotate_beads) continue;
-                const float4 V = vel_at(k);
+                if (ids[k] < P.nb && !P.srd_rotate_beads) continue;
+                const float4 V = V_[k];
                 const float3 d = scaled(V) - u;
                 const float rx = d.x * ca - d.y * sa;
                 const float ry = d.x * sa + d.y * ca;
@@ -402,9 +407,9 @@ __global__ void __launch_bounds__(kSrdThreads) srd_collide_kernel(const DevParam
             }
         }
         for (uint32_t k = 0; k < n; ++k) {
-            const uint32_t id = member(k);
+            const uint32_t id = ids[k];
             const bool is_bead = id < P.nb;
-            const float4 V = vel_at(k);
+            const float4 V = V_[k];
             float3 v = scaled(V);
             if (!is_bead || P.srd_rotate_beads) {
                 const float3 d = v - u;
@@ -416,18 +421,27 @@ __global__ void __launch_bounds__(kSrdThreads) srd_collide_kernel(const DevParam
             if (is_bead) {
                 if (lab || P.srd_rotate_beads) bvel[id] = make_float4(v.x, v.y, v.z, V.w);
             } else {
-                const float4 P4 = sp_old[id - P.nb];
+                const float4 P4 = P_[k];
                 float3 p = f3(P4);
                 const float3 dr = dt_srd * v;
                 p += dr;
                 apply_boundaries(P, p, v, dr, 0.0f);
-                const uint32_t dst = s0 + (k - nbc);
-                sp_new[dst] = make_float4(p.x, p.y, p.z, P4.w);
-                sv_new[dst] = make_float4(v.x, v.y, v.z, V.w);
+                P_[k] = make_float4(p.x, p.y, p.z, P4.w);
+                V_[k] = make_float4(v.x, v.y, v.z, V.w);
             }
         }
+        // destinations in the new solvent storage (beads: none)
+        for (uint32_t k = 0; k < n; ++k) ids[k] = k < nbc ? kEmpty : s0 + (k - nbc);
     }
-    S.srd_mean[c] = make_float4(u.x, u.y, u.z, 0.f);
+    if (valid) S.srd_mean[c] = make_float4(u.x, u.y, u.z, 0.f);
+    __syncwarp();
+    for (uint32_t k = lane; k < total; k += 32) {
+        const uint32_t d = s_id[w][k];
+        if (d != kEmpty) {
+            sp_new[d] = s_p[w][k];
+            sv_new[d] = s_v[w][k];
+        }
+    }
 }
 
 __device__ __forceinline__ float warp_allsum(float x)
@@ -437,9 +451,10 @@ __device__ __forceinline__ float warp_allsum(float x)
     return x;
 }
 
-// The collision of srd_collide_kernel for one cell of kSrdIds < n <=
-// kStableCap members, by one warp: members ranked by index in shared memory
-// (the stable order), their velocities gathered once into shared memory,
+// The collision of srd_collide_kernel for one cell of a warp that holds
+// more than kWarpCap members, by one warp: members ranked by index in shared
+// memory (the stable order; beyond kStableCap members the bucket order, and
+// the overflow is reported), velocities gathered once into shared memory,
 // sums as lane-strided partials combined by a fixed butterfly (the same
 // result on every run), then the per-member update by all lanes.
 constexpr uint32_t kBigWarps = 8;
@@ -467,22 +482,33 @@ __global__ void __launch_bounds__(256) srd_collide_big_kernel(const DevParams P,
         const uint32_t s0 = S.srd_soff[c], s1 = S.srd_soff[c + 1];
         const uint32_t nbc = b1 - b0, n = nbc + (s1 - s0);
         const uint32_t start = b0 + s0;
-        for (uint32_t k = lane; k < n; k += 32)
-            s_in[w][k] = k < nbc ? S.srd_btmp[b0 + k] : P.nb + S.srd_stmp[s0 + (k - nbc)];
-        __syncwarp();
-        for (uint32_t k = lane; k < n; k += 32) {
-            const uint32_t x = s_in[w][k];
-            uint32_t r = 0;
-            for (uint32_t j = 0; j < n; ++j) r += s_in[w][j] < x;
-            s_id[w][r] = x;
+        // beyond kStableCap members: bucket order, reported, bounded work
+        const bool fits = n <= kStableCap;
+        if (!fits && lane == 0) atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
+        auto raw = [&](uint32_t k) -> uint32_t {
+            return k < nbc ? S.srd_btmp[b0 + k] : P.nb + S.srd_stmp[s0 + (k - nbc)];
+        };
+        if (fits) {
+            for (uint32_t k = lane; k < n; k += 32) s_in[w][k] = raw(k);
+            __syncwarp();
+            for (uint32_t k = lane; k < n; k += 32) {
+                const uint32_t x = s_in[w][k];
+                uint32_t r = 0;
+                for (uint32_t j = 0; j < n; ++j) r += s_in[w][j] < x;
+                s_id[w][r] = x;
+            }
+            __syncwarp();
         }
-        __syncwarp();
+        auto member = [&](uint32_t k) -> uint32_t { return fits ? s_id[w][k] : raw(k); };
+        auto vel_of = [&](uint32_t k, uint32_t id) -> float4 {
+            return fits ? s_v[w][k] : (id < P.nb ? bvel[id] : sv_old[id - P.nb]);
+        };
         float E = 0.f;
         for (uint32_t k = lane; k < n; k += 32) {
-            const uint32_t id = s_id[w][k];
+            const uint32_t id = member(k);
             S.srd_sorted_index[start + k] = id;
             const float4 V = id < P.nb ? bvel[id] : sv_old[id - P.nb];
-            s_v[w][k] = V;
+            if (fits) s_v[w][k] = V;
             E += (0.5f * V.w) * (V.x * V.x + V.y * V.y + V.z * V.z);
         }
         __syncwarp();
@@ -490,7 +516,7 @@ __global__ void __launch_bounds__(256) srd_collide_big_kernel(const DevParams P,
         const float lam1 = lab ? sqrtf(P.srd_kT / E) : 1.0f;
         float ux = 0.f, uy = 0.f, uz = 0.f, M = 0.f;
         for (uint32_t k = lane; k < n; k += 32) {
-            const float4 V = s_v[w][k];
+            const float4 V = vel_of(k, member(k));
             const float sx = lab ? lam1 * V.x : V.x, sy = lab ? lam1 * V.y : V.y, sz = lab ? lam1 * V.z : V.z;
             ux += V.w * sx;
             uy += V.w * sy;
@@ -514,8 +540,8 @@ __global__ void __launch_bounds__(256) srd_collide_big_kernel(const DevParams P,
         if (rel) {
             float ke = 0.f, nrot = 0.f;
             for (uint32_t k = lane; k < n; k += 32) {
-                if (s_id[w][k] < P.nb && !P.srd_rotate_beads) continue;
-                const float4 V = s_v[w][k];
+                if (member(k) < P.nb && !P.srd_rotate_beads) continue;
+                const float4 V = vel_of(k, member(k));
                 const float dx = (lab ? lam1 * V.x : V.x) - ux, dy = (lab ? lam1 * V.y : V.y) - uy;
                 const float rx = dx * ca - dy * sa, ry = dx * sa + dy * ca;
                 ke += (0.5f * V.w) * (rx * rx + ry * ry);
@@ -529,9 +555,9 @@ __global__ void __launch_bounds__(256) srd_collide_big_kernel(const DevParams P,
             }
         }
         for (uint32_t k = lane; k < n; k += 32) {
-            const uint32_t id = s_id[w][k];
+            const uint32_t id = member(k);
             const bool is_bead = id < P.nb;
-            const float4 V = s_v[w][k];
+            const float4 V = vel_of(k, id);
             float3 v = lab ? make_float3(lam1 * V.x, lam1 * V.y, lam1 * V.z) : f3(V);
             if (!is_bead || P.srd_rotate_beads) {
                 const float dx = v.x - ux, dy = v.y - uy, dz = v.z - uz;

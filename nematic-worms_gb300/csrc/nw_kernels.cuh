@@ -58,7 +58,7 @@ struct StepBuffers {
     uint32_t *srd_bcount, *srd_scount, *srd_boff, *srd_soff, *srd_bchunk, *srd_schunk;
     uint32_t *srd_start, *srd_end;
     float4* srd_mean;
-    // SRD cells too full for one thread (kSrdIds < members <= kStableCap),
+    // SRD cells of warps holding more members than the warp path stages,
     // handed to srd_collide_big_kernel: srd_big[0 .. *srd_nbig)
     uint32_t *srd_big, *srd_nbig;
     uint32_t* err;
@@ -529,12 +529,13 @@ __device__ __forceinline__ float3 srd_shift_of(const DevParams& P, unsigned long
 __global__ void __launch_bounds__(256) srd_hash_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
                                                        int shift_from_step, float3 shift, uint32_t buf_sel);
 
-// One SRD cell per thread: members in stable (index) order, then the
-// reference's isokinetic thermostat (particles_kernel_impl.cuh:605-637) or
-// none, the mass-weighted cell mean (:560-594), the +/- alpha rotation of
-// (v - u) (:640-691), the relative-velocity thermostat when selected, and the
+// SRD collision, a warp per 32 consecutive cells staged in shared memory,
+// one cell per thread: members in stable (index) order, then the reference's
+// isokinetic thermostat (particles_kernel_impl.cuh:605-637) or none, the
+// mass-weighted cell mean (:560-594), the +/- alpha rotation of (v - u)
+// (:640-691), the relative-velocity thermostat when selected, and the
 // solvent's ballistic streaming by dt_srd (solvent_integrator, :145-205).
-__global__ void __launch_bounds__(256) srd_collide_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
+__global__ void __launch_bounds__(128) srd_collide_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
                                                           float dt_srd, uint32_t buf_sel);
 
 __global__ void __launch_bounds__(256) srd_scatter_kernel(const DevParams P, const StepBuffers S);
