@@ -377,7 +377,8 @@ def run_ours(args):
                 "traffic": traffic, "alg_bytes_per_launch": bytes_launch, "avg_launch_ms": dom_ms,
                 "step": {"alg_bytes": sb, "achieved": step_gbs, "frac": step_gbs / peak,
                          "note": "whole step (timed value) against the same peak"},
-                "kernel_share": {k: round(v[0] / total_prof, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}}
+                "kernel_share": {k: round(v[0] / total_prof, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
+                "kernel_avg_ms": {k: round(v[0] / v[1], 5) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}}
 
     if rank == 0:
         line = {"metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": world,
