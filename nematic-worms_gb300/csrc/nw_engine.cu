@@ -302,23 +302,39 @@ uint64_t enqueue_steps(nw_system* s, int nsteps, float dt, uint64_t first_step, 
                                         s->stream, prof, 2u);
         }
     } else {
+        // WCA pair forces depend on positions only, so a collision (which
+        // changes bead velocities) can run between the pro part of update j
+        // and its pair pass, keeping the pair/integrate chain fused; REF_DEM
+        // pair forces read velocities, so its collision follows the pair pass.
+        const bool wca = P.model == NW_MODEL_WCA_WORMS;
+        auto list = [&](uint32_t j) {
+            if (!P.vl_on) return;
+            NW_MARK("bead_list");
+            launches += launch_bead_list(P, s->B, j, s->stream);
+        };
+        auto collide = [&](uint32_t j) {
+            launches += enqueue_srd(P, s->B, s->srd_nchunks, j, dt_srd, 1, make_float3(0.f, 0.f, 0.f), s->stream,
+                                    prof, 2u);
+        };
         NW_MARK("bead_pro");
         launches += launch_bead_pro(P, s->B, 0u, dt, s->stream);
+        list(0u);
         for (int j = 0; j < nsteps; ++j) {
             const bool srd_now = srd && ((first_step + (uint64_t)j) % gap) == 0;
-            if (j == nsteps - 1 || srd_now) {
+            if (srd_now && wca) collide((uint32_t)j);
+            if (j == nsteps - 1 || (srd_now && !wca)) {
                 NW_MARK("bead_epi");
                 launches += launch_bead_epi(P, s->B, (uint32_t)j, s->stream);
-                if (srd_now)
-                    launches += enqueue_srd(P, s->B, s->srd_nchunks, (uint32_t)j, dt_srd, 1,
-                                            make_float3(0.f, 0.f, 0.f), s->stream, prof, 2u);
+                if (srd_now && !wca) collide((uint32_t)j);
                 if (j < nsteps - 1) {
                     NW_MARK("bead_pro");
                     launches += launch_bead_pro(P, s->B, (uint32_t)(j + 1), dt, s->stream);
+                    list((uint32_t)(j + 1));
                 }
             } else {
                 NW_MARK("bead_fused");
                 launches += launch_bead_fused(P, s->B, (uint32_t)j, dt, s->stream);
+                list((uint32_t)(j + 1));
             }
         }
     }

@@ -329,7 +329,7 @@ __host__ __device__ __forceinline__ size_t pro_smem(uint32_t beads, bool reverse
 template <int CAP>
 __device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& S, unsigned long long n, float dt,
                                          uint32_t fpb, bool active, uint32_t i, float3 fprev, uint32_t blk,
-                                         uint32_t nblk)
+                                         uint32_t nblk, bool insert = true)
 {
     extern __shared__ float4 sm[];
     const uint32_t L = P.L;
@@ -446,11 +446,35 @@ __device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& 
     pick2(S.tan2, out)[i] = wt ? make_float4(tg.x, tg.y, tg.z, 0.f) : pick2(S.tan2, in)[i];
     if (!finite3(f3(nP)) || !finite3(fs)) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
 
+    if (!insert) return;  // Verlet systems: bead_list_kernel fills list n when a rebuild needs it
     const uint32_t h = P.vl_on ? list_hash(P, f3(nP)) : bead_hash(P, f3(nP));
     pick2(S.hash2, out)[i] = h;
     const uint32_t slot = atomicAdd(&pick3(S.lcount, (uint32_t)(n % 3ull))[h], 1u);
     if (slot < (uint32_t)CAP) pick2(S.lslot, out)[(size_t)h * CAP + slot] = i;
     else atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
+}
+
+// The cell list of update n for a Verlet system, built only when the pair
+// pass of update n will rebuild the neighbour lists: the same predicate on
+// the same words (the displacement bound after update n), so the two always
+// agree.  Otherwise every block leaves after reading the bound.
+template <int CAP>
+__global__ void __launch_bounds__(256) bead_list_kernel(const DevParams P, const StepBuffers S, uint32_t off)
+{
+    const unsigned long long n = *S.step_base + off;
+    if (vl_bound(S, n) <= P.vl_half_skin) return;
+    const uint32_t out = (uint32_t)(n & 1ull);
+    const float4* __restrict__ pos = pick2(S.pos2, out);
+    uint32_t* hash = pick2(S.hash2, out);
+    uint32_t* cnt = pick3(S.lcount, (uint32_t)(n % 3ull));
+    uint32_t* slots = pick2(S.lslot, out);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.nb; i += gridDim.x * blockDim.x) {
+        const uint32_t h = list_hash(P, f3(pos[i]));
+        hash[i] = h;
+        const uint32_t slot = atomicAdd(cnt + h, 1u);
+        if (slot < (uint32_t)CAP) slots[(size_t)h * CAP + slot] = i;
+        else atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
+    }
 }
 
 template <int CAP, int MAXT>
@@ -461,7 +485,7 @@ __global__ void __launch_bounds__(MAXT) bead_pro_kernel(const DevParams P, const
     const uint32_t i = blockIdx.x * fpb * P.L + threadIdx.x;
     const bool active = threadIdx.x < fpb * P.L && i < P.nb;
     const float3 fprev = active ? f3(S.force[i]) : zero3();
-    pro_part<CAP>(P, S, n, dt, fpb, active, i, fprev, blockIdx.x, gridDim.x);
+    pro_part<CAP>(P, S, n, dt, fpb, active, i, fprev, blockIdx.x, gridDim.x, !P.vl_on);
 }
 
 template <int CAP, bool kRef>
@@ -494,7 +518,7 @@ __global__ void __launch_bounds__(MAXT, (MAXT == 256 && !kRef) ? 6 : 1) bead_fus
         Fn = make_float3(F.x + pair.x, F.y + pair.y, F.z + pair.z);
         if (!finite3(Fn)) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
     }
-    pro_part<CAP>(P, S, n + 1ull, dt, fpb, active, i, Fn, blockIdx.x, gridDim.x);
+    pro_part<CAP>(P, S, n + 1ull, dt, fpb, active, i, Fn, blockIdx.x, gridDim.x, !P.vl_on);
 }
 
 // A batch block: copy its replica's parameter block into shared memory and
@@ -605,6 +629,15 @@ uint64_t launch_bead_pro(const DevParams& P, const StepBuffers& B, uint32_t off,
         if (big) bead_pro_kernel<8, 1024><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb);
         else bead_pro_kernel<8, 256><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb);
     }
+    return 1;
+}
+
+uint64_t launch_bead_list(const DevParams& P, const StepBuffers& B, uint32_t off, cudaStream_t s)
+{
+    if (P.nb == 0 || !P.vl_on) return 0;
+    const uint32_t blocks = cdiv32(P.nb, 256) < 608u ? cdiv32(P.nb, 256) : 608u;  // 4 blocks per SM
+    if (B.cap == 16) bead_list_kernel<16><<<blocks, 256, 0, s>>>(P, B, off);
+    else bead_list_kernel<8><<<blocks, 256, 0, s>>>(P, B, off);
     return 1;
 }
 

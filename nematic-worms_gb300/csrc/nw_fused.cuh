@@ -10,6 +10,9 @@ uint32_t list_filaments_per_block(uint32_t L, uint32_t nf);
 
 // pro(n) with n = *step_base + off: integrate .. hash, insert into list n.
 uint64_t launch_bead_pro(const DevParams& P, const StepBuffers& B, uint32_t off, float dt, cudaStream_t s);
+// Verlet systems: the cell list of update n, built only when the pair pass
+// of update n rebuilds the neighbour lists (launch after the pro part of n).
+uint64_t launch_bead_list(const DevParams& P, const StepBuffers& B, uint32_t off, cudaStream_t s);
 // epi(n): pair forces from list n; force = complete F_n.
 uint64_t launch_bead_epi(const DevParams& P, const StepBuffers& B, uint32_t off, cudaStream_t s);
 // epi(n) followed by pro(n+1) in one kernel.
