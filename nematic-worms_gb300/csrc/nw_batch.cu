@@ -197,12 +197,23 @@ cudaError_t clean(nw_batch* b)
 uint64_t enqueue(nw_batch* b, int nsteps)
 {
     if (b->blocks == 0) return 0;
-    launch_batch(kBatchPro, b->d_slots, b->d_block_rep, b->blocks, b->threads, b->smem, b->cap, b->B, 0u, b->stream);
-    for (int j = 0; j < nsteps; ++j)
-        launch_batch(j == nsteps - 1 ? kBatchEpi : kBatchFused, b->d_slots, b->d_block_rep, b->blocks, b->threads,
-                     b->smem, b->cap, b->B, (uint32_t)j, b->stream);
+    uint64_t launches = 0;
+    auto L = [&](int mode, uint32_t off) {
+        launch_batch(mode, b->d_slots, b->d_block_rep, b->blocks, b->threads, b->smem, b->cap, b->B, off, b->stream);
+        ++launches;
+    };
+    L(kBatchPro, 0u);
+    if (b->vl) L(kBatchList, 0u);
+    for (int j = 0; j < nsteps; ++j) {
+        if (j == nsteps - 1) {
+            L(kBatchEpi, (uint32_t)j);
+        } else {
+            L(kBatchFused, (uint32_t)j);
+            if (b->vl) L(kBatchList, (uint32_t)(j + 1));
+        }
+    }
     advance_step_kernel<<<1, 1, 0, b->stream>>>(b->B.step_base, (unsigned long long)nsteps);
-    return (uint64_t)nsteps + 2ull;
+    return launches + 1ull;
 }
 
 nw_status state_ptr(nw_batch* b, int array, float4** p)

@@ -557,9 +557,20 @@ __global__ void __launch_bounds__(MAXT) batch_kernel(const ReplicaSlot* __restri
     const unsigned long long n = *S.step_base + off;
     const uint32_t i = blk * fpb * P.L + threadIdx.x;
     const bool active = threadIdx.x < fpb * P.L && i < P.nb;
+    if (MODE == kBatchList) {
+        // this replica's cell list of update n, only when its pair pass rebuilds
+        if (!P.vl_on || vl_bound(S, n) <= P.vl_half_skin || !active) return;
+        const uint32_t out = (uint32_t)(n & 1ull);
+        const uint32_t h = list_hash(P, f3(pick2(S.pos2, out)[i]));
+        pick2(S.hash2, out)[i] = h;
+        const uint32_t slot = atomicAdd(&pick3(S.lcount, (uint32_t)(n % 3ull))[h], 1u);
+        if (slot < (uint32_t)CAP) pick2(S.lslot, out)[(size_t)h * CAP + slot] = i;
+        else atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
+        return;
+    }
     if (MODE == kBatchPro) {
         const float3 fprev = active ? f3(S.force[i]) : zero3();
-        pro_part<CAP>(P, S, n, dt, fpb, active, i, fprev, blk, nblk);
+        pro_part<CAP>(P, S, n, dt, fpb, active, i, fprev, blk, nblk, !P.vl_on);
         return;
     }
     float3 Fn = zero3();
@@ -570,7 +581,7 @@ __global__ void __launch_bounds__(MAXT) batch_kernel(const ReplicaSlot* __restri
         if (!finite3(Fn)) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
         if (MODE == kBatchEpi) S.force[i] = make_float4(Fn.x, Fn.y, Fn.z, F.w);
     }
-    if (MODE == kBatchFused) pro_part<CAP>(P, S, n + 1ull, dt, fpb, active, i, Fn, blk, nblk);
+    if (MODE == kBatchFused) pro_part<CAP>(P, S, n + 1ull, dt, fpb, active, i, Fn, blk, nblk, !P.vl_on);
 }
 
 uint32_t cdiv32(uint64_t a, uint32_t b) { return (uint32_t)((a + b - 1) / b); }
@@ -587,11 +598,12 @@ void launch_batch(int mode, const ReplicaSlot* table, const uint32_t* block_rep,
         if (big) batch_kernel<CAPV, MODEV, 512><<<blocks, threads, smem, s>>>(table, block_rep, S, off);      \
         else batch_kernel<CAPV, MODEV, 256><<<blocks, threads, smem, s>>>(table, block_rep, S, off);          \
     } while (0)
-#define NW_BATCH_MODE(CAPV)                                    \
-    do {                                                       \
-        if (mode == kBatchPro) NW_BATCH(CAPV, kBatchPro);      \
-        else if (mode == kBatchEpi) NW_BATCH(CAPV, kBatchEpi); \
-        else NW_BATCH(CAPV, kBatchFused);                      \
+#define NW_BATCH_MODE(CAPV)                                      \
+    do {                                                         \
+        if (mode == kBatchPro) NW_BATCH(CAPV, kBatchPro);        \
+        else if (mode == kBatchEpi) NW_BATCH(CAPV, kBatchEpi);   \
+        else if (mode == kBatchList) NW_BATCH(CAPV, kBatchList); \
+        else NW_BATCH(CAPV, kBatchFused);                        \
     } while (0)
     if (cap == 16) NW_BATCH_MODE(16);
     else NW_BATCH_MODE(8);

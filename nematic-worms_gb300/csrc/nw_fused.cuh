@@ -35,7 +35,9 @@ struct ReplicaSlot {
     unsigned long long nbr_off;  // first neighbour-list word
 };
 
-enum BatchMode { kBatchPro = 0, kBatchEpi = 1, kBatchFused = 2 };
+// kBatchList: a replica's cell list of update n when its pair pass will
+// rebuild the Verlet lists (Verlet replicas; launched after each pro part)
+enum BatchMode { kBatchPro = 0, kBatchEpi = 1, kBatchFused = 2, kBatchList = 3 };
 
 // One launch over all replicas: block b serves replica block_rep[b].  S holds
 // the batch's base pointers; `threads` >= every replica's fpb * L.
