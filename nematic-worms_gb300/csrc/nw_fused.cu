@@ -531,6 +531,15 @@ __global__ void __launch_bounds__(MAXT) batch_kernel(const ReplicaSlot* __restri
     __shared__ DevParams sP;
     const uint32_t r = __ldg(block_rep + blockIdx.x);
     const ReplicaSlot* e = table + r;
+    if (MODE == kBatchList) {
+        // leave before staging the parameter block unless this replica rebuilds
+        if (!e->P.vl_on || !S0.vstate) return;
+        const unsigned long long n0 = *S0.step_base + off;
+        const uint32_t* vs = S0.vstate + 8u * r;
+        const float bound = __uint_as_float(vs[(uint32_t)((n0 + 1ull) & 1ull)]) +
+                            __uint_as_float(vs[2u + (uint32_t)(n0 % 3ull)]);
+        if (bound <= e->P.vl_half_skin) return;
+    }
     {
         const uint32_t* src = reinterpret_cast<const uint32_t*>(&e->P);
         uint32_t* dst = reinterpret_cast<uint32_t*>(&sP);

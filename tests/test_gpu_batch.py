@@ -48,7 +48,7 @@ def test_batch_matches_single_systems(lib, strategy, threads):
         b.sync()
         assert b.step_index == n
         # pro, (n - 1) fused, epi, step counter; Verlet batches add a list kernel after each pro part
-        assert b.last_launch_count == (2 * n + 1 if strategy == abi.NW_STRATEGY_VERLET else n + 2)
+        assert b.last_launch_count == (2 * n + 2 if strategy == abi.NW_STRATEGY_VERLET else n + 2)
         for r, c in enumerate(cfgs):
             c.neighbor_skin = 0.3
             p, v, f = run_single(c, *states[r], n, strategy)
