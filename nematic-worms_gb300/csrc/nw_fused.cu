@@ -524,7 +524,7 @@ __global__ void __launch_bounds__(MAXT, (MAXT == 256 && !kRef) ? 6 : 1) bead_fus
 // A batch block: copy its replica's parameter block into shared memory and
 // run pro, epi or fused for that replica's slice of the batch buffers.
 template <int CAP, int MODE, int MAXT>
-__global__ void __launch_bounds__(MAXT) batch_kernel(const ReplicaSlot* __restrict__ table,
+__global__ void __launch_bounds__(MAXT, MAXT == 256 ? 6 : 1) batch_kernel(const ReplicaSlot* __restrict__ table,
                                                      const uint32_t* __restrict__ block_rep, const StepBuffers S0,
                                                      uint32_t off)
 {
