@@ -41,7 +41,6 @@ struct DevParams {
     float srd_cell[3];
     float srd_alpha, srd_kT, srd_shift_lo;
     float srd_sin_a, srd_cos_a;  // sin and cos of the rotation angle alpha
-    uint32_t srd_gap;            // steps between scheduled collisions
     int32_t srd_rotate_beads, srd_thermo;
     uint32_t seed_lo, seed_hi;
     // multiply-shift divisors by grid[0] and grid[0] * grid[1] (see fast_div)

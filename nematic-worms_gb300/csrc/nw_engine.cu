@@ -63,7 +63,6 @@ DevParams make_dev_params(const NwConfig& c, float dt)
     P.srd_alpha = c.srd_alpha;
     P.srd_sin_a = (float)std::sin((double)c.srd_alpha);
     P.srd_cos_a = (float)std::cos((double)c.srd_alpha);
-    P.srd_gap = c.srd_gap ? c.srd_gap : 1u;
     P.srd_kT = c.srd_kT;
     P.srd_shift_lo = c.srd_shift_lo;
     P.srd_rotate_beads = c.srd_rotate_beads;
@@ -166,9 +165,6 @@ uint64_t enqueue_srd(const DevParams& P, const StepBuffers& B, uint32_t srd_nchu
                      int shift_from_step, float3 shift, cudaStream_t s, Prof* prof, uint32_t buf_sel)
 {
     if (P.ntotal == 0) return 0;
-    // a collision at a caller's shift hashes all solvent itself: drop the
-    // counts the previous collision precomputed for the next scheduled one
-    if (!shift_from_step) cudaMemsetAsync(B.srd_scount, 0, ((size_t)P.srd_ncells + 8) * 4, s);
     NW_MARK("srd_hash");
     srd_hash_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(P, B, step_off, shift_from_step, shift, buf_sel);
     NW_MARK("srd_chunk_sum");
@@ -182,10 +178,10 @@ uint64_t enqueue_srd(const DevParams& P, const StepBuffers& B, uint32_t srd_nchu
     NW_MARK("srd_scatter");
     srd_scatter_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(P, B);
     NW_MARK("srd_collide");
-    srd_collide_kernel<<<cdiv(P.srd_ncells, 128), 128, 0, s>>>(P, B, step_off, dt_srd, buf_sel, shift_from_step);
+    srd_collide_kernel<<<cdiv(P.srd_ncells, 128), 128, 0, s>>>(P, B, step_off, dt_srd, buf_sel);
     NW_MARK("srd_collide_big");
-    srd_collide_big_kernel<<<kSrdBigBlocks, 256, 0, s>>>(P, B, step_off, dt_srd, buf_sel, shift_from_step);
-    srd_flip_kernel<<<1, 1, 0, s>>>(P, B, step_off, shift_from_step);
+    srd_collide_big_kernel<<<kSrdBigBlocks, 256, 0, s>>>(P, B, step_off, dt_srd, buf_sel);
+    srd_flip_kernel<<<1, 1, 0, s>>>(B.scur);
     return 9;
 }
 
@@ -275,14 +271,6 @@ uint32_t collision_parity(const nw_system* s, uint64_t first, int nsteps)
 // Clear the list counters when the step counter changed under them.
 cudaError_t clean_lists(nw_system* s)
 {
-    if (s->srd_pre_dirty && s->B.srd_pre) {
-        // the solvent may have moved: the next collision hashes it from scratch
-        cudaError_t e = cudaMemsetAsync(s->B.srd_pre, 0xff, 8, s->stream);
-        if (e == cudaSuccess)
-            e = cudaMemsetAsync(s->B.srd_scount, 0, ((size_t)s->srd_ncells + 8) * 4, s->stream);
-        if (e != cudaSuccess) return e;
-        s->srd_pre_dirty = false;
-    }
     if (s->vl && s->vl_dirty) {
         // an unbounded displacement forces a list build at the next pair pass
         const uint32_t init[8] = {0x7f000000u, 0x7f000000u, 0u, 0u, 0u, 0u, 0u, 0u};
@@ -463,7 +451,6 @@ nw_status transfer(nw_system* s, int array, void* host, uint32_t start, uint32_t
         s->sorted_for = ~0ull;
         s->hash_for = ~0ull;
         if (array == NW_POSITION) s->vl_dirty = true;
-        if (array == NW_POSITION) s->srd_pre_dirty = true;
     }
     return cuda_status(e);
 }
@@ -582,7 +569,6 @@ nw_status nw_create(const NwConfig* cfg, nw_system** out)
         A(alloc_n(s, &B.srd_mean, Cs));
         A(alloc_n(s, &B.srd_big, Cs + 8));
         A(alloc_n(s, &B.srd_nbig, 4));
-        A(alloc_n(s, &B.srd_pre, 1));
     }
     A(alloc_n(s, &B.err, 4));
     A(alloc_n(s, &B.step_base, 1));
@@ -663,7 +649,6 @@ nw_status nw_set_config(nw_system* s, const NwConfig* cfg)
         if (Pn.lgrid[a] != Po.lgrid[a]) return NW_ERR_INVALID;
     s->cfg = *cfg;
     s->vl_dirty = true;  // radii or the box may have changed
-    s->srd_pre_dirty = true;
     s->hash_for = ~0ull;
     s->sorted_for = ~0ull;
     drop_graphs(s);
@@ -709,7 +694,6 @@ nw_status nw_device_array(nw_system* s, int array, void** dptr)
     case NW_POSITION:
         p = B.pos2[cur];
         s->vl_dirty = true;  // the caller may move beads through the pointer
-        s->srd_pre_dirty = true;
         s->hash_for = ~0ull;
         s->sorted_for = ~0ull;
         break;
@@ -850,7 +834,6 @@ nw_status nw_set_step(nw_system* s, uint64_t step)
         s->step = step;
         s->lists_dirty = true;
         s->vl_dirty = true;
-        s->srd_pre_dirty = true;
         s->sorted_for = ~0ull;
         s->hash_for = ~0ull;
     }

@@ -246,20 +246,25 @@ __global__ void __launch_bounds__(256) srd_hash_kernel(const DevParams P, const 
     }
     const uint32_t cur = buf_sel < 2u ? buf_sel : (uint32_t)(step & 1ull);
     const bool bead = i < P.nb;
-    // the collision before this one hashed the solvent already (scheduled collisions)
-    const bool pre = shift_from_step && *S.srd_pre == step;
-    uint32_t h = 0, key = 0xffffffffu;
-    if (valid && (bead || !pre)) {
+    uint32_t h = 0, key = 0xffffffffu;  // no cell hash reaches 2^31 - 1 with the bead bit set
+    if (valid) {
         const float4 p4 = bead ? S.pos2[cur][i] : S.spos2[*S.scur][i - P.nb];
         h = srd_hash(P, f3(p4), shift);
         S.srd_hash[i] = h;
-        key = h;
+        key = h | (bead ? 0x80000000u : 0u);
     }
-    // beads and solvent never share a warp's run (separate buckets): the
-    // warp holding both splits into two passes
-    const uint32_t sb = warp_run_slot(bead ? key : 0xffffffffu, S.srd_bcount);
-    const uint32_t ss = warp_run_slot(bead ? 0xffffffffu : key, S.srd_scount);
-    if (key != 0xffffffffu) S.srd_slot[i] = bead ? sb : ss;
+    // every lane of the warp takes part (blockDim is a multiple of 32)
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
+    const uint32_t heads = __ballot_sync(0xffffffffu, lane == 0u || prev != key);
+    const uint32_t upto = (2u << lane) - 1u;  // lanes 0..lane (all 32 bits for lane 31)
+    const uint32_t start = 31u - (uint32_t)__clz(heads & upto);
+    const uint32_t after = heads & ~upto;
+    const uint32_t end = after ? (uint32_t)(__ffs(after) - 1) : 32u;
+    uint32_t base = 0;
+    if (valid && lane == start) base = atomicAdd(bead ? &S.srd_bcount[h] : &S.srd_scount[h], end - start);
+    base = __shfl_sync(0xffffffffu, base, (int)start);
+    if (valid) S.srd_slot[i] = base + (lane - start);
 }
 
 // Bucket every particle: beads by bead index, solvent by solvent index.
@@ -294,26 +299,15 @@ constexpr uint32_t kWarpCap = 256;
 
 __global__ void __launch_bounds__(kCollideWarps * 32) srd_collide_kernel(const DevParams P, const StepBuffers S,
                                                                          uint32_t step_off, float dt_srd,
-                                                                         uint32_t buf_sel, int precompute)
+                                                                         uint32_t buf_sel)
 {
     __shared__ uint32_t s_id[kCollideWarps][kWarpCap];
     __shared__ float4 s_v[kCollideWarps][kWarpCap];
     __shared__ float4 s_p[kCollideWarps][kWarpCap];
-    __shared__ float s_next[3];
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = c < P.srd_ncells;
     const unsigned long long step = *S.step_base + step_off;
-    if (precompute) {
-        // grid shift of the next scheduled collision
-        if (threadIdx.x == 0) {
-            const float3 d = srd_shift_of(P, step + P.srd_gap);
-            s_next[0] = d.x;
-            s_next[1] = d.y;
-            s_next[2] = d.z;
-        }
-        __syncthreads();
-    }
     const uint32_t cur = buf_sel < 2u ? buf_sel : (uint32_t)(step & 1ull);
     const uint32_t a = *S.scur;
     const float4* __restrict__ sv_old = S.svel2[a];
@@ -441,23 +435,11 @@ __global__ void __launch_bounds__(kCollideWarps * 32) srd_collide_kernel(const D
     }
     if (valid) S.srd_mean[c] = make_float4(u.x, u.y, u.z, 0.f);
     __syncwarp();
-    const float3 next = precompute ? make_float3(s_next[0], s_next[1], s_next[2]) : zero3();
-    for (uint32_t k0 = 0; k0 < total; k0 += 32) {  // whole-warp iterations (slot aggregation)
-        const uint32_t k = k0 + lane;
-        const uint32_t d = k < total ? s_id[w][k] : kEmpty;
-        uint32_t key = 0xffffffffu;
+    for (uint32_t k = lane; k < total; k += 32) {
+        const uint32_t d = s_id[w][k];
         if (d != kEmpty) {
-            const float4 p4 = s_p[w][k];
-            sp_new[d] = p4;
+            sp_new[d] = s_p[w][k];
             sv_new[d] = s_v[w][k];
-            if (precompute) key = srd_hash(P, f3(p4), next);
-        }
-        if (precompute) {
-            const uint32_t slot = warp_run_slot(key, S.srd_scount);
-            if (d != kEmpty) {
-                S.srd_hash[P.nb + d] = key;
-                S.srd_slot[P.nb + d] = slot;
-            }
         }
     }
 }
@@ -477,27 +459,14 @@ __device__ __forceinline__ float warp_allsum(float x)
 // result on every run), then the per-member update by all lanes.
 constexpr uint32_t kBigWarps = 8;
 __global__ void __launch_bounds__(256) srd_collide_big_kernel(const DevParams P, const StepBuffers S,
-                                                              uint32_t step_off, float dt_srd, uint32_t buf_sel,
-                                                              int precompute)
+                                                              uint32_t step_off, float dt_srd, uint32_t buf_sel)
 {
     __shared__ uint32_t s_in[kBigWarps][kStableCap];
     __shared__ uint32_t s_id[kBigWarps][kStableCap];
     __shared__ float4 s_v[kBigWarps][kStableCap];
-    __shared__ float s_next[3];
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
     const uint32_t nbig = *S.srd_nbig;
     const unsigned long long step = *S.step_base + step_off;
-    if (nbig == 0u) return;
-    if (precompute) {
-        if (threadIdx.x == 0) {
-            const float3 d = srd_shift_of(P, step + P.srd_gap);
-            s_next[0] = d.x;
-            s_next[1] = d.y;
-            s_next[2] = d.z;
-        }
-        __syncthreads();
-    }
-    const float3 next = precompute ? make_float3(s_next[0], s_next[1], s_next[2]) : zero3();
     const uint32_t cur = buf_sel < 2u ? buf_sel : (uint32_t)(step & 1ull);
     const uint32_t a = *S.scur;
     const float4* __restrict__ sv_old = S.svel2[a];
@@ -585,40 +554,28 @@ __global__ void __launch_bounds__(256) srd_collide_big_kernel(const DevParams P,
                 scale2 = true;
             }
         }
-        for (uint32_t k0 = 0; k0 < n; k0 += 32) {  // whole-warp iterations (slot aggregation)
-            const uint32_t k = k0 + lane;
-            uint32_t key = 0xffffffffu, dst = kEmpty;
-            if (k < n) {
-                const uint32_t id = member(k);
-                const bool is_bead = id < P.nb;
-                const float4 V = vel_of(k, id);
-                float3 v = lab ? make_float3(lam1 * V.x, lam1 * V.y, lam1 * V.z) : f3(V);
-                if (!is_bead || P.srd_rotate_beads) {
-                    const float dx = v.x - ux, dy = v.y - uy, dz = v.z - uz;
-                    const float rx = dx * ca - dy * sa, ry = dx * sa + dy * ca;
-                    v = make_float3(ux + rx, uy + ry, uz + dz);
-                    if (scale2) v = make_float3(ux + lam2 * (v.x - ux), uy + lam2 * (v.y - uy), v.z);
-                }
-                if (is_bead) {
-                    if (lab || P.srd_rotate_beads) bvel[id] = make_float4(v.x, v.y, v.z, V.w);
-                } else {
-                    const float4 P4 = sp_old[id - P.nb];
-                    float3 p = f3(P4);
-                    const float3 dr = dt_srd * v;
-                    p += dr;
-                    apply_boundaries(P, p, v, dr, 0.0f);
-                    dst = s0 + (k - nbc);
-                    sp_new[dst] = make_float4(p.x, p.y, p.z, P4.w);
-                    sv_new[dst] = make_float4(v.x, v.y, v.z, V.w);
-                    if (precompute) key = srd_hash(P, p, next);
-                }
+        for (uint32_t k = lane; k < n; k += 32) {
+            const uint32_t id = member(k);
+            const bool is_bead = id < P.nb;
+            const float4 V = vel_of(k, id);
+            float3 v = lab ? make_float3(lam1 * V.x, lam1 * V.y, lam1 * V.z) : f3(V);
+            if (!is_bead || P.srd_rotate_beads) {
+                const float dx = v.x - ux, dy = v.y - uy, dz = v.z - uz;
+                const float rx = dx * ca - dy * sa, ry = dx * sa + dy * ca;
+                v = make_float3(ux + rx, uy + ry, uz + dz);
+                if (scale2) v = make_float3(ux + lam2 * (v.x - ux), uy + lam2 * (v.y - uy), v.z);
             }
-            if (precompute) {
-                const uint32_t slot = warp_run_slot(key, S.srd_scount);
-                if (dst != kEmpty) {
-                    S.srd_hash[P.nb + dst] = key;
-                    S.srd_slot[P.nb + dst] = slot;
-                }
+            if (is_bead) {
+                if (lab || P.srd_rotate_beads) bvel[id] = make_float4(v.x, v.y, v.z, V.w);
+            } else {
+                const float4 P4 = sp_old[id - P.nb];
+                float3 p = f3(P4);
+                const float3 dr = dt_srd * v;
+                p += dr;
+                apply_boundaries(P, p, v, dr, 0.0f);
+                const uint32_t dst = s0 + (k - nbc);
+                sp_new[dst] = make_float4(p.x, p.y, p.z, P4.w);
+                sv_new[dst] = make_float4(v.x, v.y, v.z, V.w);
             }
         }
         if (lane == 0) S.srd_mean[c] = make_float4(ux, uy, uz, 0.f);
@@ -627,11 +584,7 @@ __global__ void __launch_bounds__(256) srd_collide_big_kernel(const DevParams P,
 }
 
 // The collision just written the solvent to the other buffer.
-__global__ void srd_flip_kernel(const DevParams P, const StepBuffers S, uint32_t step_off, int precompute)
-{
-    *S.scur ^= 1u;
-    *S.srd_pre = precompute ? *S.step_base + step_off + P.srd_gap : ~0ull;
-}
+__global__ void srd_flip_kernel(uint32_t* scur) { *scur ^= 1u; }
 
 __global__ void advance_step_kernel(unsigned long long* step_base, unsigned long long k) { *step_base += k; }
 

@@ -61,9 +61,6 @@ struct StepBuffers {
     // SRD cells of warps holding more members than the warp path stages,
     // handed to srd_collide_big_kernel: srd_big[0 .. *srd_nbig)
     uint32_t *srd_big, *srd_nbig;
-    // the solvent's SRD hash and bucket slot of the next scheduled collision
-    // are precomputed by the collision before it, for step *srd_pre (~0: none)
-    unsigned long long* srd_pre;
     uint32_t* err;
     unsigned long long* step_base;
 };
@@ -532,24 +529,6 @@ __device__ __forceinline__ float3 srd_shift_of(const DevParams& P, unsigned long
 __global__ void __launch_bounds__(256) srd_hash_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
                                                        int shift_from_step, float3 shift, uint32_t buf_sel);
 
-// Slot of each lane's key in its bucket, one atomic per run of equal keys
-// along the warp (every lane of the warp must call; key 0xffffffff = none).
-__device__ __forceinline__ uint32_t warp_run_slot(uint32_t key, uint32_t* counts)
-{
-    const uint32_t lane = threadIdx.x & 31u;
-    const bool valid = key != 0xffffffffu;
-    const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
-    const uint32_t heads = __ballot_sync(0xffffffffu, lane == 0u || prev != key);
-    const uint32_t upto = (2u << lane) - 1u;  // lanes 0..lane (all 32 bits for lane 31)
-    const uint32_t start = 31u - (uint32_t)__clz(heads & upto);
-    const uint32_t after = heads & ~upto;
-    const uint32_t end = after ? (uint32_t)(__ffs(after) - 1) : 32u;
-    uint32_t base = 0;
-    if (valid && lane == start) base = atomicAdd(counts + key, end - start);
-    base = __shfl_sync(0xffffffffu, base, (int)start);
-    return base + (lane - start);
-}
-
 // SRD collision, a warp per 32 consecutive cells staged in shared memory,
 // one cell per thread: members in stable (index) order, then the reference's
 // isokinetic thermostat (particles_kernel_impl.cuh:605-637) or none, the
@@ -557,17 +536,14 @@ __device__ __forceinline__ uint32_t warp_run_slot(uint32_t key, uint32_t* counts
 // (:640-691), the relative-velocity thermostat when selected, and the
 // solvent's ballistic streaming by dt_srd (solvent_integrator, :145-205).
 __global__ void __launch_bounds__(128) srd_collide_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
-                                                          float dt_srd, uint32_t buf_sel, int precompute);
+                                                          float dt_srd, uint32_t buf_sel);
 
 __global__ void __launch_bounds__(256) srd_scatter_kernel(const DevParams P, const StepBuffers S);
 // One warp per SRD cell of the srd_big list (grid-stride over the list).
 __global__ void __launch_bounds__(256) srd_collide_big_kernel(const DevParams P, const StepBuffers S,
-                                                              uint32_t step_off, float dt_srd, uint32_t buf_sel,
-                                                              int precompute);
+                                                              uint32_t step_off, float dt_srd, uint32_t buf_sel);
 constexpr uint32_t kSrdBigBlocks = 608;  // 4 blocks of 8 warps per SM
-// After a collision: the solvent now lives in the other buffer, and the
-// precomputed hashes are for the collision srd_gap steps on (or none).
-__global__ void srd_flip_kernel(const DevParams P, const StepBuffers S, uint32_t step_off, int precompute);
+__global__ void srd_flip_kernel(uint32_t* scur);
 
 __global__ void advance_step_kernel(unsigned long long* step_base, unsigned long long k);
 

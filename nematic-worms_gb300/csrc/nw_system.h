@@ -32,7 +32,6 @@ struct nw_system {
     uint32_t scur = 0;            // solvent buffer holding the current solvent (mirror of *B.scur)
     bool vl = false;              // NW_STRATEGY_VERLET: hash2 holds Verlet-grid hashes
     bool vl_dirty = true;         // Verlet lists must be rebuilt at the next update
-    bool srd_pre_dirty = true;    // solvent hashes precomputed by the last collision are stale
     uint64_t hash_for = ~0ull;    // step whose reference hashes are in hash2[cur] (Verlet systems)
     std::vector<GraphEntry> graphs;
     uint64_t last_launches = 0;
