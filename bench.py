@@ -45,6 +45,9 @@ WORKLOADS = {
     # 64 replicas of the 4k-bead workload, 200-step differentiable rollout,
     # lists frozen per 20-step segment, gradient of the S / C_v loss
     "adjoint_64x4k": dict(adjoint=64),
+    # +1/2 / -1/2 defect search on a 400,000-bead frame (40,000 worms x 10
+    # beads, 8 planted defects, density 1 in a 632 x 632 box), cells of 2
+    "defects_400k": dict(defects=(40000, 10, 632.0, 2.0)),
 }
 
 
@@ -578,6 +581,100 @@ def run_adjoint(args):
     return 0
 
 
+def defect_frame(n_worms, L, box, seed=11):
+    """Worms of L beads along a director field with 8 planted +/-1/2 defects."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    sites = [(rng.uniform(0.1, 0.9) * box, rng.uniform(0.1, 0.9) * box, q) for q in (0.5, -0.5) * 4]
+    m = 0.5 * (L - 1) * 0.8 + 1.0
+    c = rng.uniform(m, box - m, (n_worms, 2))
+    a = sum(q * np.arctan2(c[:, 1] - y, c[:, 0] - x) for x, y, q in sites) + rng.normal(0, 0.2, n_worms)
+    k = np.arange(L) - 0.5 * (L - 1)
+    pos = np.zeros((n_worms * L, 4), dtype=np.float32)
+    pos[:, 0] = (c[:, None, 0] + 0.8 * k * np.cos(a)[:, None]).ravel()
+    pos[:, 1] = (c[:, None, 1] + 0.8 * k * np.sin(a)[:, None]).ravel()
+    return pos
+
+
+def run_defects(args):
+    """Defect search (director field + Burgers circuits + clustering) on one
+    frame per call, through the public call a user makes (System.find_defects:
+    device binning and circuits, host clustering), frames resident on the
+    device; the CPU arm is the numpy restatement of the reference's analysis
+    on the same frame."""
+    import numpy as np
+    import torch
+
+    import nwgb
+    from nwgb import abi
+    from nwgb.init import wca_config
+
+    rank, world, local = env_rank()
+    n_worms, L, box, cs = WORKLOADS[args.workload]["defects"]
+    pos = defect_frame(n_worms, L, box)
+    nb = len(pos)
+    steps = min(args.steps, 2000)
+
+    def cpu_time(reps):
+        sys.path.insert(0, str(REPO / "oracle"))
+        import defects_oracle
+
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            d = defects_oracle.find_defects(pos[:, :2], L, cs)
+        return (time.perf_counter() - t0) / reps, d
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        for _ in range(min(args.warmup, 1)):
+            cpu_time(1)
+        per, _ = cpu_time(max(1, min(steps, 5)))
+        line = {"metric": "frames/s", "value": 1.0 / per, "unit": "frames/s", "n_gpus": 0, "steps": steps,
+                "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True, "impl": "reference",
+                "config": {"workload": args.workload, "beads": nb, "cell_size": cs},
+                "cpu_baseline": {"value": 1.0 / per, "unit": "frames/s", "cores": 1, "kind": "port",
+                                 "sample": "the whole frame, numpy restatement of the reference's analysis"},
+                "e2e": {"value": 1.0 / per, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
+
+    torch.cuda.set_device(local)
+    cfg = wca_config(n_worms, L, (box, box), lib=None)
+    with nwgb.System(cfg) as s:
+        s.set_array(abi.NW_POSITION, pos)
+        for _ in range(args.warmup):
+            want = s.find_defects(cs)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            got = s.find_defects(cs)
+        per = (time.perf_counter() - t0) / steps
+        # end to end: the frame uploaded from pinned host memory every call
+        host = torch.from_numpy(pos).pin_memory().numpy()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            s.set_array(abi.NW_POSITION, host)
+            got = s.find_defects(cs)
+        e2e = (time.perf_counter() - t0) / steps
+    cpu_per, cpu_d = cpu_time(2) if rank == 0 and not args.no_cpu_baseline else (None, None)
+    same = cpu_d is None or (len(cpu_d) == len(got) and np.array_equal(cpu_d["x"], got["x"]))
+    line = {"metric": "frames/s", "value": 1.0 / per, "unit": "frames/s", "n_gpus": world, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32/i64", "data": "synthetic",
+            "config": {"workload": args.workload, "beads": nb, "cell_size": cs, "defects": int(len(got))},
+            "e2e": {"value": 1.0 / e2e, "unit": "frames/s", "h2d_bytes_per_step": int(pos.nbytes),
+                    "d2h_bytes_per_step": int(len(got) * 24 + 4)},
+            "gpu_launches": steps * 3, "matches_cpu": bool(same), "timing": "host wall clock per synchronous call"}
+    if cpu_per is not None:
+        line["cpu_baseline"] = {"value": 1.0 / cpu_per, "unit": "frames/s", "cores": 1, "kind": "port",
+                                "sample": "the whole frame, numpy restatement of the reference's analysis"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -597,6 +694,8 @@ def main():
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no gradients"}), flush=True)
             return 0
         return run_adjoint(args)
+    if "defects" in WORKLOADS[args.workload]:
+        return run_defects(args)
     if "batch" in WORKLOADS[args.workload]:
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched replicas; "

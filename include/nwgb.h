@@ -317,6 +317,37 @@ nw_status nw_writer_frame(nw_writer* w, int iteration, float dt);
 nw_status nw_writer_flush(nw_writer* w);
 nw_status nw_writer_close(nw_writer* w);
 
+/* ---- topological defects -------------------------------------------------- */
+
+/* +1/2 and -1/2 defects of the nematic director field of a 2D system, the
+ * reference's analysis (analysis/make_director_field.py:10-47 then
+ * analysis/find_defects.py:43-207) on the current bead positions:
+ *  - bead tangents r_{i+1} - r_{i-1}, one-sided at filament ends; the first
+ *    and the last bead of the system get none (analysis/afa/utils.py:35-49
+ *    centres its windows on beads 1 .. n-2); raw differences unless
+ *    NW_DEFECT_MIN_IMAGE asks for the minimum image;
+ *  - a grid of cells of edge cell_size from the beads' lowest x and y,
+ *    ceil((max - min + 1e-4) / cell_size) cells per axis;
+ *  - a cell's director angle is the nematic tensor's, taken in
+ *    [-pi/4, 3pi/4) (-pi/2 for a vertical director, 0 for an empty cell),
+ *    the representative the reference's eigen-solver gives;
+ *  - around every interior cell the director's rotation along the ring of its
+ *    8 neighbours, each step taken into (-pi/2, pi/2); a total beyond
+ *    pi - pi/16 in magnitude marks a defect cell of charge sign / 2;
+ *  - marked cells of one sign that touch (8-neighbourhood, no periodic wrap)
+ *    form one defect at (mean cell index) * cell_size + min + cell_size / 2.
+ * Positive defects first, each sign in order of its first cell (x-major).
+ * Binning (fixed-point sums: independent of thread order) and the circuits
+ * run on the device, the clustering of the marked cells on the host.
+ * Synchronous.  *n_out is the number of defects; at most max_out are written. */
+#define NW_DEFECT_MIN_IMAGE 1u
+typedef struct NwDefect {
+    double x, y;     /* position */
+    float charge;    /* +0.5 or -0.5 */
+    uint32_t cells;  /* marked cells merged into this defect */
+} NwDefect;
+nw_status nw_find_defects(nw_system* sys, float cell_size, uint32_t flags, NwDefect* out, int max_out, int* n_out);
+
 /* Numerics self-check of the refined reciprocal, square root and quotient
  * the force laws use (no reference counterpart).  For host arrays a[n] and
  * b[n] of positive normal floats it writes, per element, out[4*i + 0..3] =

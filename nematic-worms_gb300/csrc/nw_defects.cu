@@ -1,0 +1,263 @@
+// nw_defects.cu — +1/2 / -1/2 defects of the director field on the device
+// (include/nwgb.h, "topological defects").
+//
+// Three kernels: the beads' bounding box (float min/max through order-
+// preserving integer atomics); every bead adds cos 2a and sin 2a of its
+// tangent angle a to its grid cell as 2^30 fixed-point integers (integer
+// atomics: the sums, and so every later result, are the same whatever the
+// thread order); every interior cell sums the director's rotation along the
+// ring of its eight neighbours and lists itself when the total exceeds
+// pi - pi/16 in magnitude.  The host merges touching marked cells of one sign
+// as the reference's analysis does (analysis/find_defects.py:126-160).
+//
+// The cell of a bead is floor((r - min) / cell_size) in double precision,
+// the reference's float64 arithmetic on the same float32 positions, so beads
+// on a cell edge land where they land there.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "nw_engine.h"
+#include "nw_system.h"
+
+namespace {
+
+constexpr double kFix = 1073741824.0;  // 2^30
+constexpr float kPi = 3.14159265358979323846f;
+
+struct DefectGrid {
+    uint32_t nx, ny;
+    double cs, ox, oy;
+};
+
+// float <-> uint32 keeping the order, for min/max by integer atomics
+__device__ __forceinline__ uint32_t ord_key(float f)
+{
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+inline float ord_val(uint32_t k)
+{
+    const uint32_t u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+__global__ void __launch_bounds__(256) defect_bounds_kernel(const float4* __restrict__ pos, uint32_t nb,
+                                                            uint32_t* __restrict__ box)
+{
+    uint32_t lo_x = 0xffffffffu, lo_y = 0xffffffffu, hi_x = 0u, hi_y = 0u;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += gridDim.x * blockDim.x) {
+        const float4 r = pos[i];
+        const uint32_t kx = ord_key(r.x), ky = ord_key(r.y);
+        lo_x = min(lo_x, kx), lo_y = min(lo_y, ky), hi_x = max(hi_x, kx), hi_y = max(hi_y, ky);
+    }
+    for (int o = 16; o; o >>= 1) {
+        lo_x = min(lo_x, __shfl_xor_sync(0xffffffffu, lo_x, o));
+        lo_y = min(lo_y, __shfl_xor_sync(0xffffffffu, lo_y, o));
+        hi_x = max(hi_x, __shfl_xor_sync(0xffffffffu, hi_x, o));
+        hi_y = max(hi_y, __shfl_xor_sync(0xffffffffu, hi_y, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(box + 0, lo_x);
+        atomicMin(box + 1, lo_y);
+        atomicMax(box + 2, hi_x);
+        atomicMax(box + 3, hi_y);
+    }
+}
+
+__global__ void __launch_bounds__(256) defect_bin_kernel(const nw::DevParams P, const float4* __restrict__ pos,
+                                                         DefectGrid G, bool min_image, long long* __restrict__ acc)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.nb || i == 0 || i + 1 == P.nb) return;  // the first and last bead have no tangent
+    const uint32_t c = i % P.L;
+    const uint32_t a = c == 0 ? i : i - 1, b = c + 1 == P.L ? i : i + 1;
+    const float4 pa = pos[a], pb = pos[b], r = pos[i];
+    float3 d = make_float3(pb.x - pa.x, pb.y - pa.y, pb.z - pa.z);
+    if (min_image) nw::min_image(P, d);
+    const float q = d.x * d.x + d.y * d.y;
+    const int gx = (int)floor(((double)r.x - G.ox) / G.cs), gy = (int)floor(((double)r.y - G.oy) / G.cs);
+    if (gx < 0 || gy < 0 || gx >= (int)G.nx || gy >= (int)G.ny) return;  // not reached: the grid spans the beads
+    long long* cell = acc + 2ull * ((size_t)gx * G.ny + gy);
+    if (!(q > 0.f)) return;
+    const float c2 = (d.x * d.x - d.y * d.y) / q, s2 = (2.f * d.x * d.y) / q;  // cos 2a, sin 2a
+    atomicAdd((unsigned long long*)cell, (unsigned long long)llrint((double)c2 * kFix));
+    atomicAdd((unsigned long long*)(cell + 1), (unsigned long long)llrint((double)s2 * kFix));
+}
+
+// Director angle of a cell: the nematic tensor's, as the representative the
+// reference's eigenvector gives: [-pi/4, 3pi/4), -pi/2 for an exactly
+// vertical director (diagonal tensor), 0 for an empty or isotropic cell.
+__device__ __forceinline__ float cell_theta(const long long* acc, const DefectGrid& G, uint32_t x, uint32_t y)
+{
+    const long long* c = acc + 2ull * ((size_t)x * G.ny + y);
+    const long long C = c[0], S = c[1];
+    if (S == 0) return C < 0 ? -0.5f * kPi : 0.f;
+    float t = 0.5f * atan2f((float)((double)S / kFix), (float)((double)C / kFix));
+    if (t < -0.25f * kPi) t += kPi;
+    return t;
+}
+
+// rotation from t1 to t2 of a headless director (analysis/find_defects.py:62-68)
+__device__ __forceinline__ float theta_step(float t1, float t2)
+{
+    float d = t2 - t1;
+    if (d >= 0.5f * kPi) d -= kPi;
+    else if (d <= -0.5f * kPi) d += kPi;
+    return d;
+}
+
+__global__ void __launch_bounds__(256) defect_circuit_kernel(DefectGrid G, const long long* __restrict__ acc,
+                                                             uint32_t* __restrict__ marks, uint32_t* __restrict__ nmarks,
+                                                             uint32_t cap)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= G.nx * G.ny) return;
+    const uint32_t x = k / G.ny, y = k - x * G.ny;
+    if (x < 1 || y < 1 || x + 1 >= G.nx || y + 1 >= G.ny) return;
+    // the ring of the 8 neighbours from (+1, 0) round to (+1, 0), counter-clockwise
+    const int rx[9] = {1, 1, 0, -1, -1, -1, 0, 1, 1}, ry[9] = {0, 1, 1, 1, 0, -1, -1, -1, 0};
+    float t1 = cell_theta(acc, G, x + 1, y), total = 0.f;
+#pragma unroll
+    for (int s = 1; s < 9; ++s) {
+        const float t2 = cell_theta(acc, G, x + rx[s], y + ry[s]);
+        total += theta_step(t1, t2);
+        t1 = t2;
+    }
+    const float delta = kPi / 16.f;
+    if (total > kPi - delta || total < -kPi + delta) {
+        const uint32_t slot = atomicAdd(nmarks, 1u);
+        if (slot < cap) marks[slot] = (k << 1) | (total > 0.f ? 1u : 0u);
+    }
+}
+
+// Touching marked cells (8-neighbourhood, no wrap) of one sign merged; each
+// cluster labelled by its first cell in x-major order, the fixed point of the
+// reference's lowest-neighbour relabelling (analysis/find_defects.py:126-160).
+void cluster(const std::vector<uint32_t>& cells, uint32_t nx, uint32_t ny, std::vector<std::vector<uint32_t>>& out)
+{
+    const size_t n = cells.size();  // sorted
+    std::vector<uint32_t> parent(n);
+    for (size_t a = 0; a < n; ++a) parent[a] = (uint32_t)a;
+    auto find = [&](uint32_t a) {
+        while (parent[a] != a) a = parent[a] = parent[parent[a]];
+        return a;
+    };
+    for (size_t a = 0; a < n; ++a) {
+        const int x = (int)(cells[a] / ny), y = (int)(cells[a] % ny);
+        for (int dx = -1; dx <= 1; ++dx)
+            for (int dy = -1; dy <= 1; ++dy) {
+                const int qx = x + dx, qy = y + dy;
+                if ((dx == 0 && dy == 0) || qx < 0 || qy < 0 || qx >= (int)nx || qy >= (int)ny) continue;
+                const uint32_t q = (uint32_t)qx * ny + (uint32_t)qy;
+                const auto it = std::lower_bound(cells.begin(), cells.end(), q);
+                if (it == cells.end() || *it != q) continue;
+                const uint32_t ra = find((uint32_t)a), rb = find((uint32_t)(it - cells.begin()));
+                if (ra != rb) parent[std::max(ra, rb)] = std::min(ra, rb);
+            }
+    }
+    std::vector<int> slot(n, -1);
+    for (size_t a = 0; a < n; ++a) {
+        const uint32_t r = find((uint32_t)a);
+        if (slot[r] < 0) {
+            slot[r] = (int)out.size();
+            out.emplace_back();
+        }
+        out[slot[r]].push_back(cells[a]);
+    }
+}
+
+}  // namespace
+
+extern "C" nw_status nw_find_defects(nw_system* s, float cell_size, uint32_t flags, NwDefect* out, int max_out,
+                                     int* n_out)
+{
+    if (!s || !n_out || max_out < 0 || (max_out > 0 && !out)) return NW_ERR_INVALID;
+    if (!(cell_size > 0.f) || !std::isfinite(cell_size) || (flags & ~NW_DEFECT_MIN_IMAGE)) return NW_ERR_INVALID;
+    if (s->cfg.dim >= 3) return NW_ERR_UNSUPPORTED;
+    *n_out = 0;
+    if (s->nb == 0) return NW_OK;
+    const float4* pos = s->B.pos2[s->lists ? (uint32_t)((s->step + 1ull) & 1ull) : 0u];
+    const uint32_t cap = 1u << 16;  // marked cells reported (defects are rare)
+    uint32_t *box = nullptr, *marks = nullptr;
+    long long* acc = nullptr;
+    uint32_t hbox[5] = {0xffffffffu, 0xffffffffu, 0u, 0u, 0u};  // lo x, lo y, hi x, hi y, marked cells
+    DefectGrid G{};
+    size_t ncell = 0;
+    nw_status st = NW_OK;
+    cudaError_t e = cudaMalloc(&box, sizeof(hbox));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(box, hbox, sizeof(hbox), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) {
+        defect_bounds_kernel<<<std::min<uint32_t>((s->nb + 255) / 256, 1024), 256, 0, s->stream>>>(pos, s->nb, box);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hbox, box, sizeof(hbox), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) {
+        const double lx = ord_val(hbox[0]), ly = ord_val(hbox[1]), hx = ord_val(hbox[2]), hy = ord_val(hbox[3]);
+        const double cs = (double)cell_size;
+        const double fx = std::ceil((hx - lx + 0.0001) / cs), fy = std::ceil((hy - ly + 0.0001) / cs);
+        if (!std::isfinite(lx + ly + hx + hy) || !(fx * fy < (double)(1u << 30)))
+            st = NW_ERR_INVALID;  // non-finite positions or a grid too fine for the beads' extent
+        else {
+            G = DefectGrid{(uint32_t)fx, (uint32_t)fy, cs, lx, ly};
+            ncell = (size_t)G.nx * G.ny;
+            e = cudaMalloc(&acc, ncell * 2 * sizeof(long long));
+            if (e == cudaSuccess) e = cudaMalloc(&marks, (size_t)cap * 4);
+            if (e == cudaSuccess) e = cudaMemsetAsync(acc, 0, ncell * 2 * sizeof(long long), s->stream);
+        }
+    }
+    if (e == cudaSuccess && st == NW_OK) {
+        const nw::DevParams P = nw::make_dev_params(s->cfg, s->cfg.dt);
+        defect_bin_kernel<<<(s->nb + 255) / 256, 256, 0, s->stream>>>(P, pos, G, (flags & NW_DEFECT_MIN_IMAGE) != 0,
+                                                                       acc);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) {
+            defect_circuit_kernel<<<(uint32_t)((ncell + 255) / 256), 256, 0, s->stream>>>(G, acc, marks, box + 4,
+                                                                                           cap);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&hbox[4], box + 4, 4, cudaMemcpyDeviceToHost, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    }
+    std::vector<uint32_t> m;
+    if (e == cudaSuccess && st == NW_OK) {
+        m.resize(std::min(hbox[4], cap));
+        if (!m.empty()) e = cudaMemcpy(m.data(), marks, m.size() * 4, cudaMemcpyDeviceToHost);
+    }
+    cudaFree(box);
+    cudaFree(acc);
+    cudaFree(marks);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? NW_ERR_NOMEM : NW_ERR_CUDA;
+    }
+    if (st != NW_OK) return st;
+    if (hbox[4] > cap) return NW_ERR_CELL_OVERFLOW;
+    std::sort(m.begin(), m.end());  // x-major cell order
+    const double ox = G.ox + 0.0 + G.cs / 2.0, oy = G.oy + 0.0 + G.cs / 2.0;  // the first cell's centre
+    int n = 0;
+    for (int sign = 1; sign >= 0; --sign) {
+        std::vector<uint32_t> cells;
+        for (uint32_t v : m)
+            if ((v & 1u) == (uint32_t)sign) cells.push_back(v >> 1);
+        std::vector<std::vector<uint32_t>> clusters;
+        cluster(cells, G.nx, G.ny, clusters);
+        for (const auto& cl : clusters) {
+            double mx = 0.0, my = 0.0;
+            for (uint32_t c : cl) {
+                mx += (double)(c / G.ny);
+                my += (double)(c % G.ny);
+            }
+            mx /= (double)cl.size();
+            my /= (double)cl.size();
+            if (n < max_out) out[n] = NwDefect{mx * G.cs + ox, my * G.cs + oy, sign ? 0.5f : -0.5f, (uint32_t)cl.size()};
+            ++n;
+        }
+    }
+    *n_out = n;
+    return NW_OK;
+}

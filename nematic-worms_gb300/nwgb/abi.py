@@ -169,6 +169,15 @@ STATUS_NAMES = {
     NW_ERR_IO: "file could not be opened or written",
 }
 
+NW_DEFECT_MIN_IMAGE = 1
+
+
+class NwDefect(C.Structure):
+    """include/nwgb.h NwDefect: one +1/2 or -1/2 defect."""
+
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("charge", C.c_float), ("cells", _u32)]
+
+
 # Every symbol the library must export: (name, restype, argtypes)
 _P = C.c_void_p
 _sysp = C.c_void_p
@@ -206,6 +215,7 @@ HANDLE_API = [
     ("nw_writer_frame", C.c_int, [_P, C.c_int, _f32]),
     ("nw_writer_flush", C.c_int, [_P]),
     ("nw_writer_close", C.c_int, [_P]),
+    ("nw_find_defects", C.c_int, [_sysp, _f32, _u32, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
 ]
 
 _fp = C.c_void_p  # device pointers are passed as integers

@@ -28,7 +28,7 @@ REFERENCE_TREE = Path(os.environ.get("NW_REFERENCE_TREE", "/root/reference"))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 
-CU_SOURCES = ["nw_kernels.cu", "nw_fused.cu", "nw_engine.cu", "nw_legacy.cu", "nw_sort.cu", "nw_noalloc.cu", "nw_batch.cu", "nw_adjoint.cu", "nw_writer.cu"]
+CU_SOURCES = ["nw_kernels.cu", "nw_fused.cu", "nw_engine.cu", "nw_legacy.cu", "nw_sort.cu", "nw_noalloc.cu", "nw_batch.cu", "nw_adjoint.cu", "nw_writer.cu", "nw_defects.cu"]
 CPP_SOURCES = ["nw_config.cpp"]
 
 

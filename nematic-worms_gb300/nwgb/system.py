@@ -151,6 +151,27 @@ class System:
         check(self.lib.nw_profile_steps(self._h, int(n), float(dt), buf, 32, C.byref(cnt)), "nw_profile_steps")
         return {buf[k].name.decode(): (buf[k].total_ms, int(buf[k].launches)) for k in range(cnt.value)}
 
+    def find_defects(self, cell_size: float = 2.0, min_image: bool = False, max_defects: int = 4096) -> np.ndarray:
+        """+1/2 and -1/2 defects of the director field of the current beads
+        (analysis/find_defects.py:170-207 on the director field of
+        analysis/make_director_field.py:10-47, computed on the device).
+
+        Returns a structured array with fields x, y, charge, cells: positive
+        defects first, each sign in order of its first grid cell.  cell_size
+        is the reference's ``--cellsize`` (default 2); min_image takes bead
+        tangents through the periodic boundary (the reference does not)."""
+        buf = (abi.NwDefect * max_defects)()
+        n = C.c_int()
+        flags = abi.NW_DEFECT_MIN_IMAGE if min_image else 0
+        check(self.lib.nw_find_defects(self._h, float(cell_size), flags, buf, max_defects, C.byref(n)),
+              "nw_find_defects")
+        if n.value > max_defects:
+            return self.find_defects(cell_size, min_image, n.value)
+        out = np.zeros(n.value, dtype=[("x", "f8"), ("y", "f8"), ("charge", "f4"), ("cells", "u4")])
+        for k in range(n.value):
+            out[k] = (buf[k].x, buf[k].y, buf[k].charge, buf[k].cells)
+        return out
+
     # -- checkpoints ------------------------------------------------------------------------
     def checkpoint(self) -> bytes:
         n = C.c_size_t()
