@@ -172,6 +172,10 @@ void cluster(const std::vector<uint32_t>& cells, uint32_t nx, uint32_t ny, std::
 
 }  // namespace
 
+// Fixed workspace: 8 words of bounds and counters, then the marked cells.
+constexpr uint32_t kMarkCap = 1u << 16;  // marked cells reported (defects are rare)
+constexpr uint32_t kMarkFirst = 4096;    // marked cells copied back with the count
+
 extern "C" nw_status nw_find_defects(nw_system* s, float cell_size, uint32_t flags, NwDefect* out, int max_out,
                                      int* n_out)
 {
@@ -181,62 +185,68 @@ extern "C" nw_status nw_find_defects(nw_system* s, float cell_size, uint32_t fla
     *n_out = 0;
     if (s->nb == 0) return NW_OK;
     const float4* pos = s->B.pos2[s->lists ? (uint32_t)((s->step + 1ull) & 1ull) : 0u];
-    const uint32_t cap = 1u << 16;  // marked cells reported (defects are rare)
-    uint32_t *box = nullptr, *marks = nullptr;
-    long long* acc = nullptr;
-    uint32_t hbox[5] = {0xffffffffu, 0xffffffffu, 0u, 0u, 0u};  // lo x, lo y, hi x, hi y, marked cells
-    DefectGrid G{};
-    size_t ncell = 0;
-    nw_status st = NW_OK;
-    cudaError_t e = cudaMalloc(&box, sizeof(hbox));
-    if (e == cudaSuccess) e = cudaMemcpyAsync(box, hbox, sizeof(hbox), cudaMemcpyHostToDevice, s->stream);
+    auto fail = [](cudaError_t e) {
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? NW_ERR_NOMEM : NW_ERR_CUDA;
+    };
+    cudaError_t e = cudaSuccess;
+    if (!s->defect_fixed) e = cudaMalloc(&s->defect_fixed, 32 + (size_t)kMarkCap * 4);
+    if (e == cudaSuccess && !s->defect_host) e = cudaMallocHost(&s->defect_host, 32 + (size_t)kMarkFirst * 4);
+    if (e != cudaSuccess) return fail(e);
+    uint32_t* box = (uint32_t*)s->defect_fixed;  // lo x, lo y, hi x, hi y, marked cells
+    uint32_t* marks = box + 8;
+    uint32_t* h = s->defect_host;
+    e = cudaMemsetAsync(box, 0xff, 8, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(box + 2, 0, 12, s->stream);
     if (e == cudaSuccess) {
         defect_bounds_kernel<<<std::min<uint32_t>((s->nb + 255) / 256, 1024), 256, 0, s->stream>>>(pos, s->nb, box);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(hbox, box, sizeof(hbox), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, box, 16, cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    if (e == cudaSuccess) {
-        const double lx = ord_val(hbox[0]), ly = ord_val(hbox[1]), hx = ord_val(hbox[2]), hy = ord_val(hbox[3]);
-        const double cs = (double)cell_size;
-        const double fx = std::ceil((hx - lx + 0.0001) / cs), fy = std::ceil((hy - ly + 0.0001) / cs);
-        if (!std::isfinite(lx + ly + hx + hy) || !(fx * fy < (double)(1u << 30)))
-            st = NW_ERR_INVALID;  // non-finite positions or a grid too fine for the beads' extent
-        else {
-            G = DefectGrid{(uint32_t)fx, (uint32_t)fy, cs, lx, ly};
-            ncell = (size_t)G.nx * G.ny;
-            e = cudaMalloc(&acc, ncell * 2 * sizeof(long long));
-            if (e == cudaSuccess) e = cudaMalloc(&marks, (size_t)cap * 4);
-            if (e == cudaSuccess) e = cudaMemsetAsync(acc, 0, ncell * 2 * sizeof(long long), s->stream);
-        }
+    if (e != cudaSuccess) return fail(e);
+    const double lx = ord_val(h[0]), ly = ord_val(h[1]), hx = ord_val(h[2]), hy = ord_val(h[3]);
+    const double cs = (double)cell_size;
+    const double fx = std::ceil((hx - lx + 0.0001) / cs), fy = std::ceil((hy - ly + 0.0001) / cs);
+    if (!std::isfinite(lx + ly + hx + hy) || !(fx * fy < (double)(1u << 30)))
+        return NW_ERR_INVALID;  // non-finite positions or a grid too fine for the beads' extent
+    const DefectGrid G{(uint32_t)fx, (uint32_t)fy, cs, lx, ly};
+    const size_t ncell = (size_t)G.nx * G.ny, acc_bytes = ncell * 2 * sizeof(long long);
+    if (acc_bytes > s->defect_acc_bytes) {
+        cudaFree(s->defect_acc);
+        s->defect_acc = nullptr;
+        s->defect_acc_bytes = 0;
+        e = cudaMalloc(&s->defect_acc, acc_bytes);
+        if (e != cudaSuccess) return fail(e);
+        s->defect_acc_bytes = acc_bytes;
     }
-    if (e == cudaSuccess && st == NW_OK) {
-        const nw::DevParams P = nw::make_dev_params(s->cfg, s->cfg.dt);
+    long long* acc = (long long*)s->defect_acc;
+    const nw::DevParams P = nw::make_dev_params(s->cfg, s->cfg.dt);
+    e = cudaMemsetAsync(acc, 0, acc_bytes, s->stream);
+    if (e == cudaSuccess) {
         defect_bin_kernel<<<(s->nb + 255) / 256, 256, 0, s->stream>>>(P, pos, G, (flags & NW_DEFECT_MIN_IMAGE) != 0,
                                                                        acc);
         e = cudaGetLastError();
-        if (e == cudaSuccess) {
-            defect_circuit_kernel<<<(uint32_t)((ncell + 255) / 256), 256, 0, s->stream>>>(G, acc, marks, box + 4,
-                                                                                           cap);
-            e = cudaGetLastError();
-        }
-        if (e == cudaSuccess) e = cudaMemcpyAsync(&hbox[4], box + 4, 4, cudaMemcpyDeviceToHost, s->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     }
-    std::vector<uint32_t> m;
-    if (e == cudaSuccess && st == NW_OK) {
-        m.resize(std::min(hbox[4], cap));
-        if (!m.empty()) e = cudaMemcpy(m.data(), marks, m.size() * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) {
+        defect_circuit_kernel<<<(uint32_t)((ncell + 255) / 256), 256, 0, s->stream>>>(G, acc, marks, box + 4,
+                                                                                       kMarkCap);
+        e = cudaGetLastError();
     }
-    cudaFree(box);
-    cudaFree(acc);
-    cudaFree(marks);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return e == cudaErrorMemoryAllocation ? NW_ERR_NOMEM : NW_ERR_CUDA;
+    // the count and the first marked cells in one copy (box + 4 .. marks + kMarkFirst)
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h + 4, box + 4, 16 + (size_t)kMarkFirst * 4, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return fail(e);
+    const uint32_t nm = h[4];
+    if (nm > kMarkCap) return NW_ERR_CELL_OVERFLOW;
+    std::vector<uint32_t> m(h + 8, h + 8 + std::min(nm, kMarkFirst));
+    if (nm > kMarkFirst) {
+        m.resize(nm);
+        e = cudaMemcpy(m.data() + kMarkFirst, marks + kMarkFirst, (size_t)(nm - kMarkFirst) * 4,
+                       cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return fail(e);
     }
-    if (st != NW_OK) return st;
-    if (hbox[4] > cap) return NW_ERR_CELL_OVERFLOW;
     std::sort(m.begin(), m.end());  // x-major cell order
     const double ox = G.ox + 0.0 + G.cs / 2.0, oy = G.oy + 0.0 + G.cs / 2.0;  // the first cell's centre
     int n = 0;

@@ -233,6 +233,12 @@ void free_all(nw_system* s)
     s->graphs.clear();
     for (void* p : s->allocs) cudaFree(p);
     s->allocs.clear();
+    cudaFree(s->defect_fixed);
+    cudaFree(s->defect_acc);
+    cudaFreeHost(s->defect_host);
+    s->defect_fixed = s->defect_acc = nullptr;
+    s->defect_host = nullptr;
+    s->defect_acc_bytes = 0;
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     s->own_stream = nullptr;
 }

@@ -36,4 +36,10 @@ struct nw_system {
     std::vector<GraphEntry> graphs;
     uint64_t last_launches = 0;
     std::vector<void*> allocs;
+    // defect search workspace (nw_defects.cu): bounds, counters and marked
+    // cells (fixed), the per-cell sums (grown on demand), a pinned host copy
+    void* defect_fixed = nullptr;
+    void* defect_acc = nullptr;
+    size_t defect_acc_bytes = 0;
+    uint32_t* defect_host = nullptr;
 };

@@ -72,10 +72,12 @@ def test_min_image_tangents_through_the_boundary(lib):
     """Worms wrapped through the periodic boundary: with NW_DEFECT_MIN_IMAGE the
     tangents are the physical ones; without it the raw differences (the
     reference's) are taken."""
-    rng = np.random.default_rng(3)
+    rng = np.random.default_rng(5)
     box = 60.0
-    pos = planted_frame(rng, 3000, 6, box, [(15, 30, 0.5), (45, 30, -0.5)], jitter=0.05)
-    pos = (pos + np.float32(box / 2)) % np.float32(box)  # shifted and wrapped: worms straddle the edges
+    # a +1/2, -1/2 pair one above the other, moved against the x edge: the
+    # worms round the pair straddle the periodic boundary
+    pos = planted_frame(rng, 4000, 6, box, [(30, 20, 0.5), (30, 40, -0.5)], jitter=0.05)
+    pos[:, 0] = (pos[:, 0] + np.float32(29.0)) % np.float32(box)
     with system_with(lib, pos, 6, box=(box, box)) as s:
         raw = s.find_defects(2.0)
         img = s.find_defects(2.0, min_image=True)
