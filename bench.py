@@ -340,23 +340,27 @@ def run_ours(args):
     hv = torch.empty((nb, 4), dtype=torch.float32, pin_memory=True).numpy()
     hp[:] = sysm.get_array(abi.NW_POSITION, 0, nb)
     hv[:] = sysm.get_array(abi.NW_VELOCITY, 0, nb)
-    sysm.set_graphs(False)
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+
+    def e2e_step():
         sysm.set_array(abi.NW_POSITION, hp, 0)
         sysm.set_array(abi.NW_VELOCITY, hv, 0)
         sysm.step(1, cfg.dt)
         sysm.get_array(abi.NW_POSITION, 0, nb, out=hp)
         sysm.get_array(abi.NW_VELOCITY, 0, nb, out=hv)
+
+    for _ in range(GAP):  # one single-step graph per collision phase, built before the clock starts
+        e2e_step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
     e2e_s = time.perf_counter() - t0
     e2e_t = torch.tensor([e2e_s], device="cuda")
     if dist:
         dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
     e2e_value = nb * e2e_steps * world / float(e2e_t.item())
-    sysm.set_graphs(True)
 
     # ---- per-kernel device time (events around every launch) ---------------------------
     prof = sysm.profile(2 * chunk, cfg.dt)

@@ -1,5 +1,6 @@
 // nw_engine.cu — the handle API of include/nwgb.h: system lifetime, state
 // transfer, the step launcher with CUDA-graph replay, SRD, checkpoints.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -201,6 +202,38 @@ __global__ void __launch_bounds__(256) ref_hash_kernel(const DevParams P, const 
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < P.nb) hash[i] = bead_hash(P, f3(pos[i]));
+}
+
+// Positions set between updates of a Verlet system: staged in the free
+// position buffer, moved into the current one while the largest squared
+// displacement is taken (non-negative floats order as their bits); the
+// displacement is then added to the lists' bound, so unchanged or slightly
+// moved beads keep their lists and larger moves rebuild them.
+__global__ void __launch_bounds__(256) set_positions_kernel(const float4* __restrict__ src, float4* __restrict__ dst,
+                                                            uint32_t n, uint32_t* __restrict__ dmax)
+{
+    uint32_t m = 0u;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 a = src[i], b = dst[i];
+        const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const uint32_t bits = d2 == d2 ? __float_as_uint(d2) : 0x7f800000u;  // NaN counts as unbounded
+        m = bits > m ? bits : m;
+        dst[i] = a;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        const uint32_t t = __shfl_xor_sync(0xffffffffu, m, o);
+        m = t > m ? t : m;
+    }
+    if ((threadIdx.x & 31u) == 0u && m) atomicMax(dmax, m);
+}
+
+__global__ void vl_add_displacement_kernel(uint32_t* __restrict__ vstate, uint32_t slot)
+{
+    const float d = sqrtf(__uint_as_float(vstate[5]));
+    vstate[slot] = __float_as_uint(__uint_as_float(vstate[slot]) + d);
+    vstate[5] = 0u;
 }
 
 }  // namespace nw
@@ -437,8 +470,24 @@ nw_status transfer(nw_system* s, int array, void* host, uint32_t start, uint32_t
     cudaError_t e = cudaSuccess;
     char* h = static_cast<char*>(host);
     const uint64_t end = (uint64_t)start + count;
-    // bead part
-    if (start < nbead) {
+    // bead part; positions of a Verlet system with valid lists go through the
+    // free buffer so that the lists' displacement bound takes the move
+    bool moved_through_stage = false;
+    if (start < nbead && dir == Dir::ToDevice && array == NW_POSITION && s->vl && !s->vl_dirty &&
+        B.pos2[0] != B.pos2[1]) {
+        const uint64_t a = start, b = end < nbead ? end : nbead;
+        float4* stage = B.pos2[cur ^ 1u] + a;
+        e = cudaMemcpyAsync(stage, h, (b - a) * elem, cudaMemcpyHostToDevice, s->stream);
+        if (e == cudaSuccess) {
+            const uint32_t n = (uint32_t)(b - a);
+            const uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, 4u * 152u);
+            set_positions_kernel<<<blocks, 256, 0, s->stream>>>(stage, B.pos2[cur] + a, n, B.vstate + 5);
+            vl_add_displacement_kernel<<<1, 1, 0, s->stream>>>(B.vstate, (uint32_t)((s->step + 1ull) & 1ull));
+            e = cudaGetLastError();
+        }
+        h += (b - a) * elem;
+        moved_through_stage = true;
+    } else if (start < nbead) {
         const uint64_t a = start, b = end < nbead ? end : nbead;
         char* d = static_cast<char*>(bead_ptr) + a * elem;
         e = dir == Dir::ToDevice ? cudaMemcpyAsync(d, h, (b - a) * elem, cudaMemcpyHostToDevice, s->stream)
@@ -456,7 +505,7 @@ nw_status transfer(nw_system* s, int array, void* host, uint32_t start, uint32_t
     if (dir == Dir::ToDevice) {
         s->sorted_for = ~0ull;
         s->hash_for = ~0ull;
-        if (array == NW_POSITION) s->vl_dirty = true;
+        if (array == NW_POSITION && !moved_through_stage) s->vl_dirty = true;
     }
     return cuda_status(e);
 }
@@ -753,14 +802,14 @@ nw_status nw_step(nw_system* s, int nsteps, float dt)
     cudaError_t e = clean_lists(s);
     if (e != cudaSuccess) return cuda_status(e);
     const uint32_t phase = s->cfg.srd_enabled ? (uint32_t)(s->step % s->cfg.srd_gap) : 0u;
-    if (s->use_graphs && nsteps > 1) {
+    if (s->use_graphs) {
         uint32_t bits;
         std::memcpy(&bits, &dt, 4);
         GraphEntry* hit = nullptr;
         for (auto& g : s->graphs)
             if (g.nsteps == nsteps && g.dt_bits == bits && g.phase == phase && g.version == s->version) hit = &g;
         if (!hit) {
-            if (s->graphs.size() >= 8) drop_graphs(s);
+            if (s->graphs.size() >= 24) drop_graphs(s);  // single steps take one graph per collision phase
             cudaGraph_t graph = nullptr;
             e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
             if (e != cudaSuccess) return cuda_status(e);

@@ -336,10 +336,35 @@ __global__ void __launch_bounds__(kCollideWarps * 32) srd_collide_kernel(const D
         else if (valid) S.srd_mean[c] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
-    // members of this cell in stable order: ids < nb are beads, nb + k is solvent k
+    // members of this cell in stable order: ids < nb are beads, nb + k is solvent k.
+    // The warp's bucket entries are loaded lane-strided (consecutive cells'
+    // entries are consecutive in the buckets), each placed in its cell's
+    // segment; then every lane orders its own cell's segment in shared memory.
+    // per-cell tables in the (not yet used) position staging of this warp
+    uint32_t* s_loc = reinterpret_cast<uint32_t*>(&s_p[w][0]);
+    uint32_t* s_b0 = s_loc + 33;
+    uint32_t* s_nbc = s_loc + 65;
+    uint32_t* s_s0 = s_loc + 97;
+    s_loc[lane] = loc;
+    s_b0[lane] = b0;
+    s_nbc[lane] = nbc;
+    s_s0[lane] = s0;
+    if (lane == 31u) s_loc[32] = total;
+    __syncwarp();
+#pragma unroll 4
+    for (uint32_t j = lane; j < total; j += 32) {
+        // the cell of member slot j: the last cell whose segment starts at or before j
+        uint32_t q = 0;
+#pragma unroll
+        for (uint32_t step = 16; step; step >>= 1)
+            if (s_loc[q + step] <= j) q += step;
+        const uint32_t k = j - s_loc[q], nq = s_nbc[q];
+        s_id[w][j] = k < nq ? S.srd_btmp[s_b0[q] + k] : P.nb + S.srd_stmp[s_s0[q] + (k - nq)];
+    }
+    __syncwarp();
     uint32_t* ids = &s_id[w][loc];
-    for (uint32_t k = 0; k < n; ++k) {
-        const uint32_t x = k < nbc ? S.srd_btmp[b0 + k] : P.nb + S.srd_stmp[s0 + (k - nbc)];
+    for (uint32_t k = 1; k < n; ++k) {  // insertion sort of the cell's segment
+        const uint32_t x = ids[k];
         uint32_t m = k;
         while (m > 0 && ids[m - 1] > x) {
             ids[m] = ids[m - 1];

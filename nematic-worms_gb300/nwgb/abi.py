@@ -10,6 +10,8 @@ import ctypes as C
 import os
 from pathlib import Path
 
+import numpy as np
+
 PKG_ROOT = Path(__file__).resolve().parent.parent          # nematic-worms_gb300/
 REPO_ROOT = PKG_ROOT.parent
 LIB_DIR = PKG_ROOT / "lib"
@@ -176,6 +178,10 @@ class NwDefect(C.Structure):
     """include/nwgb.h NwDefect: one +1/2 or -1/2 defect."""
 
     _fields_ = [("x", C.c_double), ("y", C.c_double), ("charge", C.c_float), ("cells", _u32)]
+
+
+# numpy view of an NwDefect array (same 24-byte layout)
+DEFECT_DTYPE = np.dtype([("x", "<f8"), ("y", "<f8"), ("charge", "<f4"), ("cells", "<u4")])
 
 
 # Every symbol the library must export: (name, restype, argtypes)

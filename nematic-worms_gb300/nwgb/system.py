@@ -167,10 +167,7 @@ class System:
               "nw_find_defects")
         if n.value > max_defects:
             return self.find_defects(cell_size, min_image, n.value)
-        out = np.zeros(n.value, dtype=[("x", "f8"), ("y", "f8"), ("charge", "f4"), ("cells", "u4")])
-        for k in range(n.value):
-            out[k] = (buf[k].x, buf[k].y, buf[k].charge, buf[k].cells)
-        return out
+        return np.frombuffer(buf, dtype=abi.DEFECT_DTYPE, count=n.value).copy()
 
     # -- checkpoints ------------------------------------------------------------------------
     def checkpoint(self) -> bytes:

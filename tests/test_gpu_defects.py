@@ -93,7 +93,7 @@ def test_device_defects_of_a_simulated_state(lib, strategy):
     system reports."""
     import nwgb
 
-    cfg = wca_config(400, 10, (80.0, 80.0), seed=9, lib=lib)
+    cfg = wca_config(300, 10, (100.0, 100.0), seed=9, lib=lib)
     cfg.strategy = strategy
     pos, vel = initial_state(cfg, seed=9)
     with nwgb.System(cfg) as s:
