@@ -100,7 +100,8 @@ def alg_bytes(name: str, cfg) -> float:
         "stable_gather": 16.0 * nb,
         "srd_hash": 16.0 * (nb + ns) + 8.0 * (nb + ns),
         "srd_scatter": 16.0 * (nb + ns),
-        "srd_scan_cells": 16.0 * Cs,
+        # bead and solvent tables in one launch each
+        "srd_scan_cells": 24.0 * Cs,
         "srd_chunk_sum": 8.0 * Cs,
         "advance_step": 8.0,
     }

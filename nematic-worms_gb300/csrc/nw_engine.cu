@@ -142,10 +142,10 @@ uint64_t enqueue_bead_step(const DevParams& P, const StepBuffers& B, uint32_t nc
     NW_MARK("filament_pass");
     filament_pass_kernel<<<cdiv(P.nf, fpb), threads, smem, s>>>(P, B, step_off, dt, fpb);
     NW_MARK("chunk_sum");
-    chunk_sum_kernel<<<nchunks, 512, 0, s>>>(B.cell_count, P.ncells, B.chunk_count);
+    chunk_sum_kernel<<<nchunks, 512, 0, s>>>(B.cell_count, P.ncells, B.chunk_count, nullptr, nullptr);
     NW_MARK("scan_cells");
     scan_cells_kernel<true><<<nchunks, 512, 0, s>>>(B.cell_count, B.chunk_count, P.ncells, B.cell_offset, B.cell_start,
-                                                    B.cell_end);
+                                                    B.cell_end, nullptr, nullptr, nullptr);
     NW_MARK("scatter");
     scatter_kernel<<<cdiv(P.nb, 256), 256, 0, s>>>(B.hash, B.slot, B.cell_offset, B.tmp_index, P.nb);
     if (P.model == NW_MODEL_REF_DEM) {
@@ -169,13 +169,13 @@ uint64_t enqueue_srd(const DevParams& P, const StepBuffers& B, uint32_t srd_nchu
     NW_MARK("srd_hash");
     srd_hash_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(P, B, step_off, shift_from_step, shift, buf_sel);
     NW_MARK("srd_chunk_sum");
-    chunk_sum_kernel<<<srd_nchunks, 512, 0, s>>>(B.srd_bcount, P.srd_ncells, B.srd_bchunk);
-    chunk_sum_kernel<<<srd_nchunks, 512, 0, s>>>(B.srd_scount, P.srd_ncells, B.srd_schunk);
+    // bead and solvent counts side by side (grid rows 0 and 1)
+    chunk_sum_kernel<<<dim3(srd_nchunks, 2), 512, 0, s>>>(B.srd_bcount, P.srd_ncells, B.srd_bchunk, B.srd_scount,
+                                                          B.srd_schunk);
     NW_MARK("srd_scan_cells");
-    scan_cells_kernel<false><<<srd_nchunks, 512, 0, s>>>(B.srd_bcount, B.srd_bchunk, P.srd_ncells, B.srd_boff,
-                                                         nullptr, nullptr);
-    scan_cells_kernel<false><<<srd_nchunks, 512, 0, s>>>(B.srd_scount, B.srd_schunk, P.srd_ncells, B.srd_soff,
-                                                         nullptr, nullptr);
+    scan_cells_kernel<false><<<dim3(srd_nchunks, 2), 512, 0, s>>>(B.srd_bcount, B.srd_bchunk, P.srd_ncells,
+                                                                  B.srd_boff, nullptr, nullptr, B.srd_scount,
+                                                                  B.srd_schunk, B.srd_soff);
     NW_MARK("srd_scatter");
     srd_scatter_kernel<<<cdiv(P.ntotal, 256), 256, 0, s>>>(P, B);
     NW_MARK("srd_collide");
@@ -183,7 +183,7 @@ uint64_t enqueue_srd(const DevParams& P, const StepBuffers& B, uint32_t srd_nchu
     NW_MARK("srd_collide_big");
     srd_collide_big_kernel<<<kSrdBigBlocks, 256, 0, s>>>(P, B, step_off, dt_srd, buf_sel);
     srd_flip_kernel<<<1, 1, 0, s>>>(B.scur);
-    return 9;
+    return 7;
 }
 
 // Histogram of bead hashes (the counting sort's first pass, for the sorted
@@ -407,9 +407,9 @@ cudaError_t ensure_sorted(nw_system* s)
     B.hash = B.hash2[cur];
     B.pos = B.pos2[cur];
     count_hash_kernel<<<cdiv(s->nb, 256), 256, 0, s->stream>>>(B.hash, s->nb, B.cell_count, B.slot);
-    chunk_sum_kernel<<<s->nchunks, 512, 0, s->stream>>>(B.cell_count, P.ncells, B.chunk_count);
+    chunk_sum_kernel<<<s->nchunks, 512, 0, s->stream>>>(B.cell_count, P.ncells, B.chunk_count, nullptr, nullptr);
     scan_cells_kernel<true><<<s->nchunks, 512, 0, s->stream>>>(B.cell_count, B.chunk_count, P.ncells, B.cell_offset,
-                                                               B.cell_start, B.cell_end);
+                                                               B.cell_start, B.cell_end, nullptr, nullptr, nullptr);
     scatter_kernel<<<cdiv(s->nb, 256), 256, 0, s->stream>>>(B.hash, B.slot, B.cell_offset, B.tmp_index, s->nb);
     stable_gather_kernel<false><<<cdiv(s->nb, 256), 256, 0, s->stream>>>(P, B);
     cudaError_t e = cudaGetLastError();

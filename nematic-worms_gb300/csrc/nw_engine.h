@@ -35,7 +35,7 @@ DevParams make_dev_params(const NwConfig& c, float dt);
 uint64_t enqueue_bead_step(const DevParams& P, const StepBuffers& B, uint32_t nchunks, uint32_t step_off, float dt,
                            cudaStream_t s, Prof* prof = nullptr);
 
-// Enqueue one SRD collision (9 kernels).  With shift_from_step the grid
+// Enqueue one SRD collision (7 kernels).  With shift_from_step the grid
 // shift is drawn on the device from (seed, step); otherwise `shift` is used.
 // buf_sel names the bead buffer holding the current state (0 or 1), or 2 for
 // "the buffer of the update being collided" (step & 1).

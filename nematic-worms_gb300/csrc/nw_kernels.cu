@@ -105,8 +105,13 @@ __global__ void __launch_bounds__(1024) filament_pass_kernel(const DevParams P, 
 }
 
 __global__ void __launch_bounds__(512) chunk_sum_kernel(const uint32_t* __restrict__ a, uint32_t m,
-                                                        uint32_t* __restrict__ chunk)
+                                                        uint32_t* __restrict__ chunk, const uint32_t* __restrict__ a2,
+                                                        uint32_t* __restrict__ chunk2)
 {
+    if (blockIdx.y) {
+        a = a2;
+        chunk = chunk2;
+    }
     __shared__ uint32_t s_w[16];
     const uint32_t c0 = blockIdx.x * kChunk;
     uint32_t x = 0;
@@ -391,11 +396,12 @@ __global__ void __launch_bounds__(kCollideWarps * 32) srd_collide_kernel(const D
         float4* P_ = &s_p[w][loc];
         const bool lab = P.srd_thermo == NW_SRD_THERMO_REF_LAB;
         float E = 0.f;
-        for (uint32_t k = 0; k < n; ++k) {
-            const float4 V = V_[k];
-            const float3 v = f3(V);
-            E += (0.5f * V.w) * dot3(v, v);
-        }
+        if (lab)
+            for (uint32_t k = 0; k < n; ++k) {
+                const float4 V = V_[k];
+                const float3 v = f3(V);
+                E += (0.5f * V.w) * dot3(v, v);
+            }
         // reference isokinetic rule: lambda scales every member before the mean
         const float lam1 = lab ? sqrtf(P.srd_kT / E) : 1.0f;
         auto scaled = [&](float4 V) -> float3 { return lab ? make_float3(lam1 * V.x, lam1 * V.y, lam1 * V.z) : f3(V); };

@@ -10,9 +10,9 @@
 //                   gather positions (+ velocities and tangents) in cell order
 //   pair_*          pair forces over the 3x3(x3) neighbour cells
 // The cell-list and Verlet strategies (nw_fused.cu) run one fused kernel
-// per step instead.  Every srd_gap steps an SRD collision adds nine:
-//   srd_hash, chunk_sum x2, scan_cells x2 (bead and solvent buckets),
-//   srd_scatter, srd_collide, srd_collide_big, srd_flip.
+// per step instead.  Every srd_gap steps an SRD collision adds seven:
+//   srd_hash, chunk_sum and scan_cells (bead and solvent buckets side by
+//   side), srd_scatter, srd_collide, srd_collide_big, srd_flip.
 //
 // No float atomics are used anywhere: every output element has exactly one
 // writer, so repeated runs are bit-identical.
@@ -227,12 +227,22 @@ __global__ void __launch_bounds__(1024) filament_pass_kernel(const DevParams P, 
 // come from chunk_sum_kernel, so no block waits on another.
 // offset[c] = exclusive prefix, offset[ncells] = total; start/end in the
 // reference's format (0xffffffff for empty cells); counts are reset to zero.
+// A grid two blocks high scans a second array (count2, chunk_count2 ->
+// offset2; no bounds) in its second row.
 template <bool kBounds>
 __global__ void __launch_bounds__(512) scan_cells_kernel(uint32_t* __restrict__ count,
                                                          const uint32_t* __restrict__ chunk_count, uint32_t ncells,
                                                          uint32_t* __restrict__ offset, uint32_t* __restrict__ start,
-                                                         uint32_t* __restrict__ end)
+                                                         uint32_t* __restrict__ end, uint32_t* __restrict__ count2,
+                                                         const uint32_t* __restrict__ chunk_count2,
+                                                         uint32_t* __restrict__ offset2)
 {
+    if (blockIdx.y) {
+        count = count2;
+        chunk_count = chunk_count2;
+        offset = offset2;
+    }
+    const bool bounds = kBounds && blockIdx.y == 0;
     __shared__ uint32_t s_w[16];
     __shared__ uint32_t s_base;
     const uint32_t b = blockIdx.x, tid = threadIdx.x, lane = tid & 31u, wid = tid >> 5;
@@ -283,7 +293,7 @@ __global__ void __launch_bounds__(512) scan_cells_kernel(uint32_t* __restrict__ 
         }
         *reinterpret_cast<uint4*>(offset + c0) = make_uint4(o[0], o[1], o[2], o[3]);
         *reinterpret_cast<uint4*>(offset + c0 + 4) = make_uint4(o[4], o[5], o[6], o[7]);
-        if (kBounds) {
+        if (bounds) {
             uint32_t s[8], e[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
@@ -303,7 +313,7 @@ __global__ void __launch_bounds__(512) scan_cells_kernel(uint32_t* __restrict__ 
             const uint32_t c = c0 + k;
             if (c < ncells) {
                 offset[c] = run;
-                if (kBounds) {
+                if (bounds) {
                     start[c] = cnt[k] ? run : kEmpty;
                     end[c] = cnt[k] ? run + cnt[k] : kEmpty;
                 }
@@ -316,9 +326,11 @@ __global__ void __launch_bounds__(512) scan_cells_kernel(uint32_t* __restrict__ 
 }
 
 // Sum of each 4096-entry chunk of the cell counts (feeds scan_cells_kernel,
-// whose blocks then need no communication with one another).
+// whose blocks then need no communication with one another).  A grid two
+// blocks high does a second array (a2 -> chunk2) in its second row.
 __global__ void __launch_bounds__(512) chunk_sum_kernel(const uint32_t* __restrict__ a, uint32_t m,
-                                                        uint32_t* __restrict__ chunk);
+                                                        uint32_t* __restrict__ chunk, const uint32_t* __restrict__ a2,
+                                                        uint32_t* __restrict__ chunk2);
 
 // ---- K3: scatter into cell buckets (arbitrary order inside a bucket) -------------
 __global__ void __launch_bounds__(256) scatter_kernel(const uint32_t* __restrict__ hash,

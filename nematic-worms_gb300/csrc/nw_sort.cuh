@@ -68,8 +68,9 @@ inline void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, const R
     uint32_t *ki = keys, *vi = vals, *ko = S.keys_alt, *vo = S.vals_alt;
     for (int shift = 0; shift < 32; shift += 8) {
         radix_hist_kernel<<<nblocks, 256, 0, s>>>(ki, n, shift, S.ghist, nblocks);
-        chunk_sum_kernel<<<nchunks, 512, 0, s>>>(S.ghist, m, S.chunk);
-        scan_cells_kernel<false><<<nchunks, 512, 0, s>>>(S.ghist, S.chunk, m, S.goffset, nullptr, nullptr);
+        chunk_sum_kernel<<<nchunks, 512, 0, s>>>(S.ghist, m, S.chunk, nullptr, nullptr);
+        scan_cells_kernel<false><<<nchunks, 512, 0, s>>>(S.ghist, S.chunk, m, S.goffset, nullptr, nullptr, nullptr,
+                                                          nullptr, nullptr);
         radix_scatter_kernel<<<nblocks, 256, 0, s>>>(ki, vi, ko, vo, n, shift, S.goffset, nblocks);
         uint32_t* t = ki;
         ki = ko;

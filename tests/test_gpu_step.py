@@ -146,7 +146,7 @@ CASES = ["wca", "wca_srd", "wca_srd_dense", "wca_reverse", "wca_3d", "ref", "ref
 STRATEGIES = [abi.NW_STRATEGY_CELL_LISTS, abi.NW_STRATEGY_SORTED, abi.NW_STRATEGY_VERLET]
 # launches of one update: (bead step, SRD collision) + the step counter; Verlet systems
 # add the on-demand cell-list kernel
-LAUNCHES = {abi.NW_STRATEGY_CELL_LISTS: (2, 9), abi.NW_STRATEGY_SORTED: (6, 9), abi.NW_STRATEGY_VERLET: (3, 9)}
+LAUNCHES = {abi.NW_STRATEGY_CELL_LISTS: (2, 7), abi.NW_STRATEGY_SORTED: (6, 7), abi.NW_STRATEGY_VERLET: (3, 7)}
 
 
 def strategy_applies(kind, strategy):
