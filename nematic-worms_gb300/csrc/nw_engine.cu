@@ -181,7 +181,7 @@ uint64_t enqueue_srd(const DevParams& P, const StepBuffers& B, uint32_t srd_nchu
     NW_MARK("srd_collide");
     srd_collide_kernel<<<cdiv(P.srd_ncells, 128), 128, 0, s>>>(P, B, step_off, dt_srd, buf_sel);
     NW_MARK("srd_collide_big");
-    srd_collide_big_kernel<<<kSrdBigBlocks, 256, 0, s>>>(P, B, step_off, dt_srd, buf_sel);
+    srd_collide_big_kernel<<<kSrdBigBlocks, kBigWarps * 32, 0, s>>>(P, B, step_off, dt_srd, buf_sel);
     srd_flip_kernel<<<1, 1, 0, s>>>(B.scur);
     return 7;
 }
@@ -312,7 +312,8 @@ cudaError_t clean_lists(nw_system* s)
 {
     if (s->vl && s->vl_dirty) {
         // an unbounded displacement forces a list build at the next pair pass
-        const uint32_t init[8] = {0x7f000000u, 0x7f000000u, 0u, 0u, 0u, 0u, 0u, 0u};
+        // (and every list's counters treated as filled, so each is cleared before use)
+        const uint32_t init[8] = {0x7f000000u, 0x7f000000u, 0u, 0u, 0u, 0u, 7u, 0u};
         cudaError_t e = cudaMemcpyAsync(s->B.vstate, init, sizeof(init), cudaMemcpyHostToDevice, s->stream);
         if (e != cudaSuccess) return e;
         s->vl_dirty = false;
@@ -385,6 +386,24 @@ uint64_t enqueue_steps(nw_system* s, int nsteps, float dt, uint64_t first_step, 
 
 // Sorted order and cell bounds of the current bead hashes (cell-list systems
 // keep no sorted order between updates; this runs the counting sort once).
+// Systems whose step does not store tangents (pro_flags) compute them from
+// the current positions when they are read.
+bool lazy_tangents(const nw_system* s)
+{
+    return s->lists && (pro_flags(make_dev_params(s->cfg, s->cfg.dt)) & kProLazyTangent) != 0u;
+}
+
+cudaError_t materialize_tangents(nw_system* s)
+{
+    if (!s->tan_stale) return cudaSuccess;
+    const DevParams P = make_dev_params(s->cfg, s->cfg.dt);
+    const uint32_t cur = cur_buffer(s);
+    launch_bead_tangents(P, s->B.pos2[cur], s->B.tan2[cur], s->stream);
+    const cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) s->tan_stale = false;
+    return e;
+}
+
 cudaError_t ensure_hash(nw_system* s)
 {
     if (!s->vl || s->hash_for == s->step || s->nb == 0) return cudaSuccess;
@@ -432,7 +451,12 @@ nw_status transfer(nw_system* s, int array, void* host, uint32_t start, uint32_t
     switch (array) {
     case NW_POSITION: bead_ptr = B.pos2[cur]; solv_ptr = B.spos2[s->scur]; ntot = s->ntotal; break;
     case NW_VELOCITY: bead_ptr = B.vel2[cur]; solv_ptr = B.svel2[s->scur]; ntot = s->ntotal; break;
-    case NW_TANGENT: bead_ptr = B.tan2[cur]; break;
+    case NW_TANGENT: {
+        cudaError_t e = materialize_tangents(s);  // also before a partial write
+        if (e != cudaSuccess) return cuda_status(e);
+        bead_ptr = B.tan2[cur];
+        break;
+    }
     case NW_FORCE: bead_ptr = B.force; break;
     case NW_FORCE_OLD: bead_ptr = B.force_old; break;
     case NW_HASH: {
@@ -753,7 +777,13 @@ nw_status nw_device_array(nw_system* s, int array, void** dptr)
         s->sorted_for = ~0ull;
         break;
     case NW_VELOCITY: p = B.vel2[cur]; break;
-    case NW_TANGENT: p = B.tan2[cur]; break;
+    case NW_TANGENT: {
+        cudaError_t e = materialize_tangents(s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) return cuda_status(e);
+        p = B.tan2[cur];
+        break;
+    }
     case NW_FORCE: p = B.force; break;
     case NW_FORCE_OLD: p = B.force_old; break;
     case NW_HASH: {
@@ -832,6 +862,7 @@ nw_status nw_step(nw_system* s, int nsteps, float dt)
     if (e != cudaSuccess) return cuda_status(e);
     s->scur ^= collision_parity(s, s->step, nsteps);
     s->step += (uint64_t)nsteps;
+    if (lazy_tangents(s)) s->tan_stale = true;
     return NW_OK;
 }
 
@@ -1018,6 +1049,7 @@ nw_status nw_profile_steps(nw_system* s, int nsteps, float dt, NwKernelTime* out
     }
     s->scur ^= collision_parity(s, s->step, nsteps);
     s->step += (uint64_t)nsteps;
+    if (lazy_tangents(s)) s->tan_stale = true;
     int n = 0;
     for (size_t k = 0; k + 1 < prof.events.size(); ++k) {
         float ms = 0.f;

@@ -329,7 +329,7 @@ __host__ __device__ __forceinline__ size_t pro_smem(uint32_t beads, bool reverse
 template <int CAP>
 __device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& S, unsigned long long n, float dt,
                                          uint32_t fpb, bool active, uint32_t i, float3 fprev, uint32_t blk,
-                                         uint32_t nblk, bool insert = true)
+                                         uint32_t nblk, bool insert = true, uint32_t pflags = 0u)
 {
     extern __shared__ float4 sm[];
     const uint32_t L = P.L;
@@ -341,7 +341,8 @@ __device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& 
     float4* smx = sm + (P.reverse_on ? 3u : 1u) * beads;    // triple forces [3][beads]
 
     // lists of update n+1 must start empty: clear them while nobody reads them
-    {
+    // (with kProClearDirty only when a list build filled them since)
+    if (!(pflags & kProClearDirty) || ((S.vstate[6] >> (uint32_t)((n + 1ull) % 3ull)) & 1u)) {
         uint32_t* nxt = pick3(S.lcount, (uint32_t)((n + 1ull) % 3ull));
         const uint32_t stride = nblk * blockDim.x;
         for (uint32_t c = blk * blockDim.x + t; c < P.lncells; c += stride) nxt[c] = 0u;
@@ -420,7 +421,8 @@ __device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& 
     }
     bool wt = false;
     float3 tg = zero3();
-    if (L >= 3) {
+    const bool eager_tan = !(pflags & kProLazyTangent);
+    if (eager_tan && L >= 3) {
         if (c == 0) {
             tg = tangent_of(P, f3(R[0]), f3(R[1]));
             wt = true;
@@ -443,7 +445,7 @@ __device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& 
     pick2(S.vel2, out)[i] = nV;
     S.force_old[i] = nFo;
     S.force[i] = make_float4(fs.x, fs.y, fs.z, 0.f);
-    pick2(S.tan2, out)[i] = wt ? make_float4(tg.x, tg.y, tg.z, 0.f) : pick2(S.tan2, in)[i];
+    if (eager_tan) pick2(S.tan2, out)[i] = wt ? make_float4(tg.x, tg.y, tg.z, 0.f) : pick2(S.tan2, in)[i];
     if (!finite3(f3(nP)) || !finite3(fs)) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
 
     if (!insert) return;  // Verlet systems: bead_list_kernel fills list n when a rebuild needs it
@@ -462,7 +464,14 @@ template <int CAP>
 __global__ void __launch_bounds__(256) bead_list_kernel(const DevParams P, const StepBuffers S, uint32_t off)
 {
     const unsigned long long n = *S.step_base + off;
-    if (vl_bound(S, n) <= P.vl_half_skin) return;
+    const bool rebuild = !(vl_bound(S, n) <= P.vl_half_skin);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        // whether list n's counters hold counts: the pro part that next
+        // targets them (an earlier launch has read the bit) clears them
+        const uint32_t bit = 1u << (uint32_t)(n % 3ull);
+        S.vstate[6] = rebuild ? (S.vstate[6] | bit) : (S.vstate[6] & ~bit);
+    }
+    if (!rebuild) return;
     const uint32_t out = (uint32_t)(n & 1ull);
     const float4* __restrict__ pos = pick2(S.pos2, out);
     uint32_t* hash = pick2(S.hash2, out);
@@ -479,13 +488,13 @@ __global__ void __launch_bounds__(256) bead_list_kernel(const DevParams P, const
 
 template <int CAP, int MAXT>
 __global__ void __launch_bounds__(MAXT) bead_pro_kernel(const DevParams P, const StepBuffers S, uint32_t off, float dt,
-                                                        uint32_t fpb)
+                                                        uint32_t fpb, uint32_t pflags)
 {
     const unsigned long long n = *S.step_base + off;
     const uint32_t i = blockIdx.x * fpb * P.L + threadIdx.x;
     const bool active = threadIdx.x < fpb * P.L && i < P.nb;
     const float3 fprev = active ? f3(S.force[i]) : zero3();
-    pro_part<CAP>(P, S, n, dt, fpb, active, i, fprev, blockIdx.x, gridDim.x, !P.vl_on);
+    pro_part<CAP>(P, S, n, dt, fpb, active, i, fprev, blockIdx.x, gridDim.x, !P.vl_on, pflags);
 }
 
 template <int CAP, bool kRef>
@@ -506,7 +515,7 @@ __global__ void __launch_bounds__(256) bead_epi_kernel(const DevParams P, const 
 // epi(n) then pro(n+1): the complete force of update n stays in a register.
 template <int CAP, bool kRef, int MAXT>
 __global__ void __launch_bounds__(MAXT, (MAXT == 256 && !kRef) ? 6 : 1) bead_fused_kernel(const DevParams P, const StepBuffers S, uint32_t off,
-                                                          float dt, uint32_t fpb)
+                                                          float dt, uint32_t fpb, uint32_t pflags)
 {
     const unsigned long long n = *S.step_base + off;
     const uint32_t i = blockIdx.x * fpb * P.L + threadIdx.x;
@@ -518,7 +527,7 @@ __global__ void __launch_bounds__(MAXT, (MAXT == 256 && !kRef) ? 6 : 1) bead_fus
         Fn = make_float3(F.x + pair.x, F.y + pair.y, F.z + pair.z);
         if (!finite3(Fn)) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
     }
-    pro_part<CAP>(P, S, n + 1ull, dt, fpb, active, i, Fn, blockIdx.x, gridDim.x, !P.vl_on);
+    pro_part<CAP>(P, S, n + 1ull, dt, fpb, active, i, Fn, blockIdx.x, gridDim.x, !P.vl_on, pflags);
 }
 
 // A batch block: copy its replica's parameter block into shared memory and
@@ -643,13 +652,36 @@ uint64_t launch_bead_pro(const DevParams& P, const StepBuffers& B, uint32_t off,
     pro_shape(P, fpb, threads, smem);
     const uint32_t blocks = cdiv32(P.nf, fpb);
     const bool big = threads > 256;  // filaments longer than 256 beads: one per block, up to 1024 threads
+    const uint32_t pf = pro_flags(P);
     if (B.cap == 16) {
-        if (big) bead_pro_kernel<16, 1024><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb);
-        else bead_pro_kernel<16, 256><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb);
+        if (big) bead_pro_kernel<16, 1024><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb, pf);
+        else bead_pro_kernel<16, 256><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb, pf);
     } else {
-        if (big) bead_pro_kernel<8, 1024><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb);
-        else bead_pro_kernel<8, 256><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb);
+        if (big) bead_pro_kernel<8, 1024><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb, pf);
+        else bead_pro_kernel<8, 256><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb, pf);
     }
+    return 1;
+}
+
+// Bead tangents of the current positions, as the pro part writes them
+// (systems whose step leaves them to be computed when read).
+__global__ void __launch_bounds__(256) bead_tangent_kernel(const DevParams P, const float4* __restrict__ pos,
+                                                           float4* __restrict__ tan)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.nb) return;
+    const uint32_t L = P.L, c = i % L, b = i - c;
+    float3 tg;
+    if (c == 0) tg = tangent_of(P, f3(pos[b]), f3(pos[b + 1]));
+    else if (c == L - 1) tg = tangent_of(P, f3(pos[b + L - 2]), f3(pos[b + L - 1]));
+    else tg = tangent_of(P, f3(pos[i - 1]), f3(pos[i + 1]));
+    tan[i] = make_float4(tg.x, tg.y, tg.z, 0.f);
+}
+
+uint64_t launch_bead_tangents(const DevParams& P, const float4* pos, float4* tan, cudaStream_t s)
+{
+    if (P.nb == 0) return 0;
+    bead_tangent_kernel<<<cdiv32(P.nb, 256), 256, 0, s>>>(P, pos, tan);
     return 1;
 }
 
@@ -686,10 +718,11 @@ uint64_t launch_bead_fused(const DevParams& P, const StepBuffers& B, uint32_t of
     const uint32_t blocks = cdiv32(P.nf, fpb);
     const bool ref = P.model == NW_MODEL_REF_DEM;
     const bool big = threads > 256;
-#define NW_FUSED(CAPV, REFV)                                                                        \
-    do {                                                                                            \
-        if (big) bead_fused_kernel<CAPV, REFV, 1024><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb); \
-        else bead_fused_kernel<CAPV, REFV, 256><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb);      \
+    const uint32_t pf = pro_flags(P);
+#define NW_FUSED(CAPV, REFV)                                                                             \
+    do {                                                                                                 \
+        if (big) bead_fused_kernel<CAPV, REFV, 1024><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb, pf); \
+        else bead_fused_kernel<CAPV, REFV, 256><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb, pf);      \
     } while (0)
     if (B.cap == 16) {
         if (ref) NW_FUSED(16, true);

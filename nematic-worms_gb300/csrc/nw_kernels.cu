@@ -297,12 +297,15 @@ __global__ void __launch_bounds__(256) srd_scatter_kernel(const DevParams P, con
 // (v - u) (:640-691), the relative-velocity thermostat when selected, and the
 // solvent's ballistic streaming by dt_srd (solvent_integrator, :145-205).
 // Beads are written in place, the solvent to the other solvent buffer.
-// Warps holding more than kWarpCap members hand their cells to
-// srd_collide_big_kernel (a warp per cell).
+// A warp holding more than kWarpCap members takes its cells in rounds that
+// fit; a single cell above kWarpCap goes to srd_collide_big_kernel (a warp
+// per cell).
 constexpr int kCollideWarps = 4;
-constexpr uint32_t kWarpCap = 256;
+// 192 members per warp (32 cells at up to 6 members on average) keeps
+// 8 blocks of 4 warps resident per SM (27 KB of shared memory, 64 registers).
+constexpr uint32_t kWarpCap = 192;
 
-__global__ void __launch_bounds__(kCollideWarps * 32) srd_collide_kernel(const DevParams P, const StepBuffers S,
+__global__ void __launch_bounds__(kCollideWarps * 32, 8) srd_collide_kernel(const DevParams P, const StepBuffers S,
                                                                          uint32_t step_off, float dt_srd,
                                                                          uint32_t buf_sel)
 {
@@ -336,142 +339,157 @@ __global__ void __launch_bounds__(kCollideWarps * 32) srd_collide_kernel(const D
     const uint32_t incl = warp_incl_scan(n);
     const uint32_t loc = incl - n;  // this cell's members in the warp's range
     const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    if (total == 0u || total > kWarpCap) {  // uniform over the warp
-        if (valid && n > 0u) S.srd_big[atomicAdd(S.srd_nbig, 1u)] = c;
-        else if (valid) S.srd_mean[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (total == 0u) {  // uniform over the warp
+        if (valid) S.srd_mean[c] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
-    // members of this cell in stable order: ids < nb are beads, nb + k is solvent k.
-    // The warp's bucket entries are loaded lane-strided (consecutive cells'
-    // entries are consecutive in the buckets), each placed in its cell's
-    // segment; then every lane orders its own cell's segment in shared memory.
-    // per-cell tables in the (not yet used) position staging of this warp
-    uint32_t* s_loc = reinterpret_cast<uint32_t*>(&s_p[w][0]);
-    uint32_t* s_b0 = s_loc + 33;
-    uint32_t* s_nbc = s_loc + 65;
-    uint32_t* s_s0 = s_loc + 97;
-    s_loc[lane] = loc;
-    s_b0[lane] = b0;
-    s_nbc[lane] = nbc;
-    s_s0[lane] = s0;
-    if (lane == 31u) s_loc[32] = total;
-    __syncwarp();
-#pragma unroll 4
-    for (uint32_t j = lane; j < total; j += 32) {
-        // the cell of member slot j: the last cell whose segment starts at or before j
-        uint32_t q = 0;
-#pragma unroll
-        for (uint32_t step = 16; step; step >>= 1)
-            if (s_loc[q + step] <= j) q += step;
-        const uint32_t k = j - s_loc[q], nq = s_nbc[q];
-        s_id[w][j] = k < nq ? S.srd_btmp[s_b0[q] + k] : P.nb + S.srd_stmp[s_s0[q] + (k - nq)];
-    }
-    __syncwarp();
-    uint32_t* ids = &s_id[w][loc];
-    for (uint32_t k = 1; k < n; ++k) {  // insertion sort of the cell's segment
-        const uint32_t x = ids[k];
-        uint32_t m = k;
-        while (m > 0 && ids[m - 1] > x) {
-            ids[m] = ids[m - 1];
-            --m;
-        }
-        ids[m] = x;
-    }
-    __syncwarp();
     const uint32_t wstart = __shfl_sync(0xffffffffu, start, 0);
-    for (uint32_t k = lane; k < total; k += 32) {
-        const uint32_t id = s_id[w][k];
-        S.srd_sorted_index[wstart + k] = id;
-        if (id < P.nb) {
-            s_v[w][k] = bvel[id];
-        } else {
-            s_v[w][k] = sv_old[id - P.nb];
-            s_p[w][k] = sp_old[id - P.nb];
+    // a cell above the warp's staging capacity goes to srd_collide_big_kernel
+    if (valid && n > kWarpCap) S.srd_big[atomicAdd(S.srd_nbig, 1u)] = c;
+    // Rounds of consecutive cells whose members fit the staging buffers
+    // (one round unless the warp holds more than kWarpCap members).
+    uint32_t first = 0;
+    while (first < 32u) {
+        const uint32_t base = __shfl_sync(0xffffffffu, loc, (int)first);
+        const uint32_t fm = __ballot_sync(0xffffffffu, lane >= first && loc + n - base <= kWarpCap);
+        if (!((fm >> first) & 1u)) {  // cell `first` alone is above the capacity
+            ++first;
+            continue;
         }
-    }
-    __syncwarp();
-    float3 u = zero3();
-    if (n > 0) {
-        float4* V_ = &s_v[w][loc];
-        float4* P_ = &s_p[w][loc];
-        const bool lab = P.srd_thermo == NW_SRD_THERMO_REF_LAB;
-        float E = 0.f;
-        if (lab)
-            for (uint32_t k = 0; k < n; ++k) {
-                const float4 V = V_[k];
-                const float3 v = f3(V);
-                E += (0.5f * V.w) * dot3(v, v);
+        const uint32_t last = 31u - (uint32_t)__clz(fm);
+        const uint32_t rtotal = __shfl_sync(0xffffffffu, loc + n, (int)last) - base;
+        const bool mine = lane >= first && lane <= last;
+        // members of the round's cells in stable order: ids < nb are beads, nb + k
+        // is solvent k.  The bucket entries are loaded lane-strided (consecutive
+        // cells' entries are consecutive in the buckets), each into its cell's
+        // segment; then every lane orders its own cell's segment in shared memory.
+#pragma unroll 2
+        for (uint32_t j0 = 0; j0 < rtotal; j0 += 32u) {
+            const uint32_t j = j0 + lane, slot = base + (j < rtotal ? j : 0u);
+            uint32_t q = 0;  // the last cell whose segment starts at or before slot
+#pragma unroll
+            for (uint32_t st = 16; st; st >>= 1) {
+                const uint32_t lq = __shfl_sync(0xffffffffu, loc, (int)(q + st));
+                if (lq <= slot) q += st;
             }
-        // reference isokinetic rule: lambda scales every member before the mean
-        const float lam1 = lab ? sqrtf(P.srd_kT / E) : 1.0f;
-        auto scaled = [&](float4 V) -> float3 { return lab ? make_float3(lam1 * V.x, lam1 * V.y, lam1 * V.z) : f3(V); };
-        float M = 0.f;
-        for (uint32_t k = 0; k < n; ++k) {
-            const float4 V = V_[k];
-            u += V.w * scaled(V);
-            M += V.w;
-        }
-        if (M > 0.f) {
-            const float inv = 1.0f / M;
-            u = u * inv;
-        }
-        // rotation by +alpha or -alpha with equal probability
-        const bool plus = u01(rng_draw(P, c, step, kRngSrdRot).x) > 0.5f;
-        const float sa = plus ? P.srd_sin_a : -P.srd_sin_a, ca = P.srd_cos_a;
-        float lam2 = 1.0f;
-        bool scale2 = false;
-        if (P.srd_thermo == NW_SRD_THERMO_CELL_REL) {
-            uint32_t nrot = 0;
-            float ke = 0.f;
-            for (uint32_t k = 0; k < n; ++k) {
-                if (ids[k] < P.nb && !P.srd_rotate_beads) continue;
-                const float4 V = V_[k];
-                const float3 d = scaled(V) - u;
-                const float rx = d.x * ca - d.y * sa;
-                const float ry = d.x * sa + d.y * ca;
-                ke += (0.5f * V.w) * (rx * rx + ry * ry);
-                ++nrot;
-            }
-            if (nrot >= 2u && ke > 0.f) {
-                lam2 = sqrtf(((float)(nrot - 1u) * P.srd_kT) / ke);
-                scale2 = true;
+            const uint32_t lq = __shfl_sync(0xffffffffu, loc, (int)q), nq = __shfl_sync(0xffffffffu, nbc, (int)q);
+            const uint32_t bq = __shfl_sync(0xffffffffu, b0, (int)q), sq = __shfl_sync(0xffffffffu, s0, (int)q);
+            if (j < rtotal) {
+                const uint32_t k = slot - lq;
+                s_id[w][j] = k < nq ? S.srd_btmp[bq + k] : P.nb + S.srd_stmp[sq + (k - nq)];
             }
         }
-        for (uint32_t k = 0; k < n; ++k) {
-            const uint32_t id = ids[k];
-            const bool is_bead = id < P.nb;
-            const float4 V = V_[k];
-            float3 v = scaled(V);
-            if (!is_bead || P.srd_rotate_beads) {
-                const float3 d = v - u;
-                const float rx = d.x * ca - d.y * sa;
-                const float ry = d.x * sa + d.y * ca;
-                v = make_float3(u.x + rx, u.y + ry, u.z + d.z);
-                if (scale2) v = make_float3(u.x + lam2 * (v.x - u.x), u.y + lam2 * (v.y - u.y), v.z);
+        __syncwarp();
+        if (mine) {
+            uint32_t* ids = &s_id[w][loc - base];
+            for (uint32_t k = 1; k < n; ++k) {  // insertion sort of the cell's segment
+                const uint32_t x = ids[k];
+                uint32_t m = k;
+                while (m > 0 && ids[m - 1] > x) {
+                    ids[m] = ids[m - 1];
+                    --m;
+                }
+                ids[m] = x;
             }
-            if (is_bead) {
-                if (lab || P.srd_rotate_beads) bvel[id] = make_float4(v.x, v.y, v.z, V.w);
+        }
+        __syncwarp();
+        for (uint32_t k = lane; k < rtotal; k += 32) {
+            const uint32_t id = s_id[w][k];
+            S.srd_sorted_index[wstart + base + k] = id;
+            if (id < P.nb) {
+                s_v[w][k] = bvel[id];
             } else {
-                const float4 P4 = P_[k];
-                float3 p = f3(P4);
-                const float3 dr = dt_srd * v;
-                p += dr;
-                apply_boundaries(P, p, v, dr, 0.0f);
-                P_[k] = make_float4(p.x, p.y, p.z, P4.w);
-                V_[k] = make_float4(v.x, v.y, v.z, V.w);
+                s_v[w][k] = sv_old[id - P.nb];
+                s_p[w][k] = sp_old[id - P.nb];
             }
         }
-        // destinations in the new solvent storage (beads: none)
-        for (uint32_t k = 0; k < n; ++k) ids[k] = k < nbc ? kEmpty : s0 + (k - nbc);
-    }
-    if (valid) S.srd_mean[c] = make_float4(u.x, u.y, u.z, 0.f);
-    __syncwarp();
-    for (uint32_t k = lane; k < total; k += 32) {
-        const uint32_t d = s_id[w][k];
-        if (d != kEmpty) {
-            sp_new[d] = s_p[w][k];
-            sv_new[d] = s_v[w][k];
+        __syncwarp();
+        float3 u = zero3();
+        if (mine && n > 0) {
+            uint32_t* ids = &s_id[w][loc - base];
+            float4* V_ = &s_v[w][loc - base];
+            float4* P_ = &s_p[w][loc - base];
+            const bool lab = P.srd_thermo == NW_SRD_THERMO_REF_LAB;
+            float E = 0.f;
+            if (lab)
+                for (uint32_t k = 0; k < n; ++k) {
+                    const float4 V = V_[k];
+                    const float3 v = f3(V);
+                    E += (0.5f * V.w) * dot3(v, v);
+                }
+            // reference isokinetic rule: lambda scales every member before the mean
+            const float lam1 = lab ? sqrtf(P.srd_kT / E) : 1.0f;
+            auto scaled = [&](float4 V) -> float3 { return lab ? make_float3(lam1 * V.x, lam1 * V.y, lam1 * V.z) : f3(V); };
+            float M = 0.f;
+            for (uint32_t k = 0; k < n; ++k) {
+                const float4 V = V_[k];
+                u += V.w * scaled(V);
+                M += V.w;
+            }
+            if (M > 0.f) {
+                const float inv = 1.0f / M;
+                u = u * inv;
+            }
+            // rotation by +alpha or -alpha with equal probability
+            const bool plus = u01(rng_draw(P, c, step, kRngSrdRot).x) > 0.5f;
+            const float sa = plus ? P.srd_sin_a : -P.srd_sin_a, ca = P.srd_cos_a;
+            float lam2 = 1.0f;
+            bool scale2 = false;
+            if (P.srd_thermo == NW_SRD_THERMO_CELL_REL) {
+                uint32_t nrot = 0;
+                float ke = 0.f;
+                for (uint32_t k = 0; k < n; ++k) {
+                    if (ids[k] < P.nb && !P.srd_rotate_beads) continue;
+                    const float4 V = V_[k];
+                    const float3 d = scaled(V) - u;
+                    const float rx = d.x * ca - d.y * sa;
+                    const float ry = d.x * sa + d.y * ca;
+                    ke += (0.5f * V.w) * (rx * rx + ry * ry);
+                    ++nrot;
+                }
+                if (nrot >= 2u && ke > 0.f) {
+                    lam2 = sqrtf(((float)(nrot - 1u) * P.srd_kT) / ke);
+                    scale2 = true;
+                }
+            }
+            for (uint32_t k = 0; k < n; ++k) {
+                const uint32_t id = ids[k];
+                const bool is_bead = id < P.nb;
+                const float4 V = V_[k];
+                float3 v = scaled(V);
+                if (!is_bead || P.srd_rotate_beads) {
+                    const float3 d = v - u;
+                    const float rx = d.x * ca - d.y * sa;
+                    const float ry = d.x * sa + d.y * ca;
+                    v = make_float3(u.x + rx, u.y + ry, u.z + d.z);
+                    if (scale2) v = make_float3(u.x + lam2 * (v.x - u.x), u.y + lam2 * (v.y - u.y), v.z);
+                }
+                if (is_bead) {
+                    if (lab || P.srd_rotate_beads) bvel[id] = make_float4(v.x, v.y, v.z, V.w);
+                } else {
+                    const float4 P4 = P_[k];
+                    float3 p = f3(P4);
+                    const float3 dr = dt_srd * v;
+                    p += dr;
+                    apply_boundaries(P, p, v, dr, 0.0f);
+                    P_[k] = make_float4(p.x, p.y, p.z, P4.w);
+                    V_[k] = make_float4(v.x, v.y, v.z, V.w);
+                }
+            }
+            // destinations in the new solvent storage (beads: none)
+            for (uint32_t k = 0; k < n; ++k) ids[k] = k < nbc ? kEmpty : s0 + (k - nbc);
         }
+        if (mine && valid) S.srd_mean[c] = make_float4(u.x, u.y, u.z, 0.f);
+        __syncwarp();
+        for (uint32_t k = lane; k < rtotal; k += 32) {
+            const uint32_t d = s_id[w][k];
+            if (d != kEmpty) {
+                sp_new[d] = s_p[w][k];
+                sv_new[d] = s_v[w][k];
+            }
+        }
+        __syncwarp();
+        first = last + 1u;
     }
 }
 
@@ -482,19 +500,19 @@ __device__ __forceinline__ float warp_allsum(float x)
     return x;
 }
 
-// The collision of srd_collide_kernel for one cell of a warp that holds
-// more than kWarpCap members, by one warp: members ranked by index in shared
-// memory (the stable order; beyond kStableCap members the bucket order, and
-// the overflow is reported), velocities gathered once into shared memory,
-// sums as lane-strided partials combined by a fixed butterfly (the same
-// result on every run), then the per-member update by all lanes.
-constexpr uint32_t kBigWarps = 8;
-__global__ void __launch_bounds__(256) srd_collide_big_kernel(const DevParams P, const StepBuffers S,
-                                                              uint32_t step_off, float dt_srd, uint32_t buf_sel)
+// The collision of srd_collide_kernel for one cell of more than kWarpCap
+// members, by one warp: members ranked by index in shared memory (the stable
+// order; beyond kBigCap members the bucket order, and the overflow is
+// reported), velocities gathered once into shared memory, sums as
+// lane-strided partials combined by a fixed butterfly (the same result on
+// every run), then the per-member update by all lanes.
+__global__ void __launch_bounds__(kBigWarps * 32) srd_collide_big_kernel(const DevParams P, const StepBuffers S,
+                                                                         uint32_t step_off, float dt_srd,
+                                                                         uint32_t buf_sel)
 {
-    __shared__ uint32_t s_in[kBigWarps][kStableCap];
-    __shared__ uint32_t s_id[kBigWarps][kStableCap];
-    __shared__ float4 s_v[kBigWarps][kStableCap];
+    __shared__ uint32_t s_in[kBigWarps][kBigCap];
+    __shared__ uint32_t s_id[kBigWarps][kBigCap];
+    __shared__ float4 s_v[kBigWarps][kBigCap];
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
     const uint32_t nbig = *S.srd_nbig;
     const unsigned long long step = *S.step_base + step_off;
@@ -513,8 +531,8 @@ __global__ void __launch_bounds__(256) srd_collide_big_kernel(const DevParams P,
         const uint32_t s0 = S.srd_soff[c], s1 = S.srd_soff[c + 1];
         const uint32_t nbc = b1 - b0, n = nbc + (s1 - s0);
         const uint32_t start = b0 + s0;
-        // beyond kStableCap members: bucket order, reported, bounded work
-        const bool fits = n <= kStableCap;
+        // beyond kBigCap members: bucket order, reported, bounded work
+        const bool fits = n <= kBigCap;
         if (!fits && lane == 0) atomicOr(S.err, (uint32_t)NW_EFLAG_CELL_OVERFLOW);
         auto raw = [&](uint32_t k) -> uint32_t {
             return k < nbc ? S.srd_btmp[b0 + k] : P.nb + S.srd_stmp[s0 + (k - nbc)];

@@ -554,7 +554,9 @@ __global__ void __launch_bounds__(256) srd_scatter_kernel(const DevParams P, con
 // One warp per SRD cell of the srd_big list (grid-stride over the list).
 __global__ void __launch_bounds__(256) srd_collide_big_kernel(const DevParams P, const StepBuffers S,
                                                               uint32_t step_off, float dt_srd, uint32_t buf_sel);
-constexpr uint32_t kSrdBigBlocks = 608;  // 4 blocks of 8 warps per SM
+constexpr uint32_t kSrdBigBlocks = 608;  // 4 blocks per SM
+constexpr uint32_t kBigWarps = 4;        // warps (cells at a time) per block of srd_collide_big_kernel
+constexpr uint32_t kBigCap = 384;        // members of a cell ordered exactly by srd_collide_big_kernel
 __global__ void srd_flip_kernel(uint32_t* scur);
 
 __global__ void advance_step_kernel(unsigned long long* step_base, unsigned long long k);

@@ -33,6 +33,7 @@ struct nw_system {
     bool vl = false;              // NW_STRATEGY_VERLET: hash2 holds Verlet-grid hashes
     bool vl_dirty = true;         // Verlet lists must be rebuilt at the next update
     uint64_t hash_for = ~0ull;    // step whose reference hashes are in hash2[cur] (Verlet systems)
+    bool tan_stale = false;       // tangents not stored by the step: computed when read
     std::vector<GraphEntry> graphs;
     uint64_t last_launches = 0;
     std::vector<void*> allocs;
