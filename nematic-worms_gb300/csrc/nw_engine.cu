@@ -312,8 +312,7 @@ cudaError_t clean_lists(nw_system* s)
 {
     if (s->vl && s->vl_dirty) {
         // an unbounded displacement forces a list build at the next pair pass
-        // (and every list's counters treated as filled, so each is cleared before use)
-        const uint32_t init[8] = {0x7f000000u, 0x7f000000u, 0u, 0u, 0u, 0u, 7u, 0u};
+        const uint32_t init[8] = {0x7f000000u, 0x7f000000u, 0u, 0u, 0u, 0u, 0u, 0u};
         cudaError_t e = cudaMemcpyAsync(s->B.vstate, init, sizeof(init), cudaMemcpyHostToDevice, s->stream);
         if (e != cudaSuccess) return e;
         s->vl_dirty = false;

@@ -341,8 +341,7 @@ __device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& 
     float4* smx = sm + (P.reverse_on ? 3u : 1u) * beads;    // triple forces [3][beads]
 
     // lists of update n+1 must start empty: clear them while nobody reads them
-    // (with kProClearDirty only when a list build filled them since)
-    if (!(pflags & kProClearDirty) || ((S.vstate[6] >> (uint32_t)((n + 1ull) % 3ull)) & 1u)) {
+    {
         uint32_t* nxt = pick3(S.lcount, (uint32_t)((n + 1ull) % 3ull));
         const uint32_t stride = nblk * blockDim.x;
         for (uint32_t c = blk * blockDim.x + t; c < P.lncells; c += stride) nxt[c] = 0u;
@@ -464,14 +463,7 @@ template <int CAP>
 __global__ void __launch_bounds__(256) bead_list_kernel(const DevParams P, const StepBuffers S, uint32_t off)
 {
     const unsigned long long n = *S.step_base + off;
-    const bool rebuild = !(vl_bound(S, n) <= P.vl_half_skin);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        // whether list n's counters hold counts: the pro part that next
-        // targets them (an earlier launch has read the bit) clears them
-        const uint32_t bit = 1u << (uint32_t)(n % 3ull);
-        S.vstate[6] = rebuild ? (S.vstate[6] | bit) : (S.vstate[6] & ~bit);
-    }
-    if (!rebuild) return;
+    if (vl_bound(S, n) <= P.vl_half_skin) return;
     const uint32_t out = (uint32_t)(n & 1ull);
     const float4* __restrict__ pos = pick2(S.pos2, out);
     uint32_t* hash = pick2(S.hash2, out);

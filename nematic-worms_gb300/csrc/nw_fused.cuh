@@ -9,13 +9,10 @@ namespace nw {
 //   kProLazyTangent  tangents are not stored by the step (WCA worms of more
 //                    than three beads, whose step never reads them); the
 //                    handle API computes them when they are read
-//   kProClearDirty   list counters are cleared only when a list build has
-//                    filled them since (Verlet systems; vstate[6] holds one
-//                    bit per list)
-constexpr uint32_t kProLazyTangent = 1u, kProClearDirty = 2u;
+constexpr uint32_t kProLazyTangent = 1u;
 __host__ __device__ __forceinline__ uint32_t pro_flags(const DevParams& P)
 {
-    return (P.model == NW_MODEL_WCA_WORMS && P.L > 3u ? kProLazyTangent : 0u) | (P.vl_on ? kProClearDirty : 0u);
+    return P.model == NW_MODEL_WCA_WORMS && P.L > 3u ? kProLazyTangent : 0u;
 }
 // Tangents of the current positions as the pro part computes them.
 uint64_t launch_bead_tangents(const DevParams& P, const float4* pos, float4* tan, cudaStream_t s);

@@ -298,12 +298,14 @@ __global__ void __launch_bounds__(256) srd_scatter_kernel(const DevParams P, con
 // solvent's ballistic streaming by dt_srd (solvent_integrator, :145-205).
 // Beads are written in place, the solvent to the other solvent buffer.
 // A warp holding more than kWarpCap members takes its cells in rounds that
-// fit; a single cell above kWarpCap goes to srd_collide_big_kernel (a warp
-// per cell).
+// fit.  A cell of more than kLaneCap members goes to srd_collide_big_kernel
+// (a warp per cell), so that no lane's serial loops run far longer than its
+// neighbours'.
 constexpr int kCollideWarps = 4;
 // 192 members per warp (32 cells at up to 6 members on average) keeps
 // 8 blocks of 4 warps resident per SM (27 KB of shared memory, 64 registers).
 constexpr uint32_t kWarpCap = 192;
+static_assert(kLaneCap <= kWarpCap, "a cell of the warp path fits the staging alone");
 
 __global__ void __launch_bounds__(kCollideWarps * 32, 8) srd_collide_kernel(const DevParams P, const StepBuffers S,
                                                                          uint32_t step_off, float dt_srd,
@@ -330,32 +332,31 @@ __global__ void __launch_bounds__(kCollideWarps * 32, 8) srd_collide_kernel(cons
         s0 = S.srd_soff[c];
         nsc = S.srd_soff[c + 1] - s0;
     }
-    const uint32_t n = nbc + nsc;
+    const uint32_t nall = nbc + nsc;
     const uint32_t start = b0 + s0;  // particles before this cell in the stable order
     if (valid) {
-        S.srd_start[c] = n ? start : kEmpty;
-        S.srd_end[c] = n ? start + n : kEmpty;
+        S.srd_start[c] = nall ? start : kEmpty;
+        S.srd_end[c] = nall ? start + nall : kEmpty;
     }
+    // a cell of more than kLaneCap members is collided by a whole warp in
+    // srd_collide_big_kernel; here it counts as empty
+    const bool big = nall > kLaneCap;
+    if (valid && big) S.srd_big[atomicAdd(S.srd_nbig, 1u)] = c;
+    const uint32_t n = big ? 0u : nall;
     const uint32_t incl = warp_incl_scan(n);
-    const uint32_t loc = incl - n;  // this cell's members in the warp's range
+    const uint32_t loc = incl - n;  // this cell's members in the warp's staging
     const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
     if (total == 0u) {  // uniform over the warp
-        if (valid) S.srd_mean[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (valid && !big) S.srd_mean[c] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
-    const uint32_t wstart = __shfl_sync(0xffffffffu, start, 0);
-    // a cell above the warp's staging capacity goes to srd_collide_big_kernel
-    if (valid && n > kWarpCap) S.srd_big[atomicAdd(S.srd_nbig, 1u)] = c;
+    const uint32_t gdelta = start - loc;  // stable-order position of staged slot j of this cell: gdelta + j
     // Rounds of consecutive cells whose members fit the staging buffers
     // (one round unless the warp holds more than kWarpCap members).
     uint32_t first = 0;
     while (first < 32u) {
         const uint32_t base = __shfl_sync(0xffffffffu, loc, (int)first);
         const uint32_t fm = __ballot_sync(0xffffffffu, lane >= first && loc + n - base <= kWarpCap);
-        if (!((fm >> first) & 1u)) {  // cell `first` alone is above the capacity
-            ++first;
-            continue;
-        }
         const uint32_t last = 31u - (uint32_t)__clz(fm);
         const uint32_t rtotal = __shfl_sync(0xffffffffu, loc + n, (int)last) - base;
         const bool mine = lane >= first && lane <= last;
@@ -393,14 +394,24 @@ __global__ void __launch_bounds__(kCollideWarps * 32, 8) srd_collide_kernel(cons
             }
         }
         __syncwarp();
-        for (uint32_t k = lane; k < rtotal; k += 32) {
-            const uint32_t id = s_id[w][k];
-            S.srd_sorted_index[wstart + base + k] = id;
-            if (id < P.nb) {
-                s_v[w][k] = bvel[id];
-            } else {
-                s_v[w][k] = sv_old[id - P.nb];
-                s_p[w][k] = sp_old[id - P.nb];
+        for (uint32_t j0 = 0; j0 < rtotal; j0 += 32u) {
+            const uint32_t j = j0 + lane, slot = base + (j < rtotal ? j : 0u);
+            uint32_t q = 0;  // the cell of slot, as above
+#pragma unroll
+            for (uint32_t st = 16; st; st >>= 1) {
+                const uint32_t lq = __shfl_sync(0xffffffffu, loc, (int)(q + st));
+                if (lq <= slot) q += st;
+            }
+            const uint32_t gq = __shfl_sync(0xffffffffu, gdelta, (int)q);
+            if (j < rtotal) {
+                const uint32_t id = s_id[w][j];
+                S.srd_sorted_index[gq + slot] = id;
+                if (id < P.nb) {
+                    s_v[w][j] = bvel[id];
+                } else {
+                    s_v[w][j] = sv_old[id - P.nb];
+                    s_p[w][j] = sp_old[id - P.nb];
+                }
             }
         }
         __syncwarp();
@@ -479,7 +490,7 @@ __global__ void __launch_bounds__(kCollideWarps * 32, 8) srd_collide_kernel(cons
             // destinations in the new solvent storage (beads: none)
             for (uint32_t k = 0; k < n; ++k) ids[k] = k < nbc ? kEmpty : s0 + (k - nbc);
         }
-        if (mine && valid) S.srd_mean[c] = make_float4(u.x, u.y, u.z, 0.f);
+        if (mine && valid && !big) S.srd_mean[c] = make_float4(u.x, u.y, u.z, 0.f);
         __syncwarp();
         for (uint32_t k = lane; k < rtotal; k += 32) {
             const uint32_t d = s_id[w][k];
@@ -500,7 +511,7 @@ __device__ __forceinline__ float warp_allsum(float x)
     return x;
 }
 
-// The collision of srd_collide_kernel for one cell of more than kWarpCap
+// The collision of srd_collide_kernel for one cell of more than kLaneCap
 // members, by one warp: members ranked by index in shared memory (the stable
 // order; beyond kBigCap members the bucket order, and the overflow is
 // reported), velocities gathered once into shared memory, sums as

@@ -555,6 +555,7 @@ __global__ void __launch_bounds__(256) srd_scatter_kernel(const DevParams P, con
 __global__ void __launch_bounds__(256) srd_collide_big_kernel(const DevParams P, const StepBuffers S,
                                                               uint32_t step_off, float dt_srd, uint32_t buf_sel);
 constexpr uint32_t kSrdBigBlocks = 608;  // 4 blocks per SM
+constexpr uint32_t kLaneCap = 16;        // members of a cell collided by one lane of srd_collide_kernel
 constexpr uint32_t kBigWarps = 4;        // warps (cells at a time) per block of srd_collide_big_kernel
 constexpr uint32_t kBigCap = 384;        // members of a cell ordered exactly by srd_collide_big_kernel
 __global__ void srd_flip_kernel(uint32_t* scur);

@@ -35,13 +35,19 @@ def make_case(kind: str, lib):
         pos, vel = initial_state(cfg, seed=2)
         tan = np.zeros((cfg.n_beads, 4), np.float32)
     elif kind == "wca_srd_dense":
-        # 24 solvent per SRD cell: most cells take the warp-per-cell collision
+        # 24 solvent per SRD cell: cells take the warp-per-cell collision
         cfg = wca_config(80, 10, (40.0, 40.0), srd=True, srd_density=24.0, seed=6, lib=lib)
         pos, vel = initial_state(cfg, seed=6)
         tan = np.zeros((cfg.n_beads, 4), np.float32)
+    elif kind == "wca_srd_rounds":
+        # about 9 solvent per SRD cell: warps hold more members than their
+        # staging and collide their cells in two or three rounds
+        cfg = wca_config(80, 10, (40.0, 40.0), srd=True, srd_density=9.0, seed=7, lib=lib)
+        pos, vel = initial_state(cfg, seed=7)
+        tan = np.zeros((cfg.n_beads, 4), np.float32)
     elif kind == "wca_srd_packed":
-        # about 215 solvent per SRD cell: cells above the warp path's 192-member
-        # staging take the warp-per-cell collision, the rest one-cell rounds
+        # about 215 solvent per SRD cell: every cell takes the warp-per-cell
+        # collision, which orders up to 384 members exactly
         cfg = wca_config(12, 10, (16.0, 16.0), srd=True, srd_density=215.0, seed=8, lib=lib)
         pos, vel = initial_state(cfg, seed=8)
         tan = np.zeros((cfg.n_beads, 4), np.float32)
@@ -148,7 +154,7 @@ def run_oracle(orc, cfg, pos, vel, tan, nsteps=1, prec=32):
     return st
 
 
-CASES = ["wca", "wca_srd", "wca_srd_dense", "wca_srd_packed", "wca_reverse", "wca_3d", "ref", "ref_srd", "ref_walls", "ref_3d"]
+CASES = ["wca", "wca_srd", "wca_srd_dense", "wca_srd_rounds", "wca_srd_packed", "wca_reverse", "wca_3d", "ref", "ref_srd", "ref_walls", "ref_3d"]
 STRATEGIES = [abi.NW_STRATEGY_CELL_LISTS, abi.NW_STRATEGY_SORTED, abi.NW_STRATEGY_VERLET]
 # launches of one update: (bead step, SRD collision) + the step counter; Verlet systems
 # add the on-demand cell-list kernel
