@@ -48,6 +48,7 @@ struct nw_batch {
     std::vector<void*> state_allocs, list_allocs;
     uint64_t step = 0, version = 1, last_launches = 0;
     bool use_graphs = true, vl = false, vl_dirty = true, lists_dirty = true;
+    bool tan_stale = false;  // tangents of lazy replicas (pro_flags) computed when read
     std::vector<BatchGraph> graphs;
 };
 
@@ -229,6 +230,22 @@ nw_status state_ptr(nw_batch* b, int array, float4** p)
     }
 }
 
+// Tangents of the replicas whose step does not store them, from the current
+// positions (as the single-system engine does when they are read).
+cudaError_t materialize_tangents(nw_batch* b)
+{
+    if (!b->tan_stale) return cudaSuccess;
+    const uint32_t cur = cur_buffer(b);
+    for (int r = 0; r < b->R; ++r) {
+        const DevParams& P = b->slots[r].P;
+        if (pro_flags(P) & kProLazyTangent)
+            launch_bead_tangents(P, b->B.pos2[cur] + b->boff[r], b->B.tan2[cur] + b->boff[r], b->stream);
+    }
+    const cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) b->tan_stale = false;
+    return e;
+}
+
 nw_status set_step(nw_batch* b, uint64_t step)
 {
     const uint32_t from = cur_buffer(b);
@@ -366,6 +383,10 @@ static nw_status batch_transfer(nw_batch* b, int r, int array, void* host, uint3
     const nw_status st = state_ptr(b, array, &base);
     if (st != NW_OK) return st;
     if (!count) return NW_OK;
+    if (array == NW_TANGENT) {
+        const cudaError_t m = materialize_tangents(b);  // also before a partial write
+        if (m != cudaSuccess) return cuda_st(m);
+    }
     float4* d = base + b->boff[r] + start;
     cudaError_t e = to_dev ? cudaMemcpyAsync(d, host, (size_t)count * 16, cudaMemcpyHostToDevice, b->stream)
                            : cudaMemcpyAsync(host, d, (size_t)count * 16, cudaMemcpyDeviceToHost, b->stream);
@@ -391,6 +412,11 @@ nw_status nw_batch_device_array(nw_batch* b, int array, void** dptr)
     const nw_status st = state_ptr(b, array, &p);
     if (st != NW_OK) return st;
     if (array == NW_POSITION) b->vl_dirty = true;  // the caller may move beads through it
+    if (array == NW_TANGENT) {
+        cudaError_t e = materialize_tangents(b);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+        if (e != cudaSuccess) return cuda_st(e);
+    }
     *dptr = p;
     return NW_OK;
 }
@@ -428,6 +454,7 @@ nw_status nw_batch_step(nw_batch* b, int nsteps)
     }
     if (e != cudaSuccess) return cuda_st(e);
     b->step += (uint64_t)nsteps;
+    b->tan_stale = true;
     return NW_OK;
 }
 

@@ -580,7 +580,7 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 6 : 1) batch_kernel(const 
     }
     if (MODE == kBatchPro) {
         const float3 fprev = active ? f3(S.force[i]) : zero3();
-        pro_part<CAP>(P, S, n, dt, fpb, active, i, fprev, blk, nblk, !P.vl_on);
+        pro_part<CAP>(P, S, n, dt, fpb, active, i, fprev, blk, nblk, !P.vl_on, pro_flags(P));
         return;
     }
     float3 Fn = zero3();
@@ -591,7 +591,7 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 6 : 1) batch_kernel(const 
         if (!finite3(Fn)) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
         if (MODE == kBatchEpi) S.force[i] = make_float4(Fn.x, Fn.y, Fn.z, F.w);
     }
-    if (MODE == kBatchFused) pro_part<CAP>(P, S, n + 1ull, dt, fpb, active, i, Fn, blk, nblk, !P.vl_on);
+    if (MODE == kBatchFused) pro_part<CAP>(P, S, n + 1ull, dt, fpb, active, i, Fn, blk, nblk, !P.vl_on, pro_flags(P));
 }
 
 uint32_t cdiv32(uint64_t a, uint32_t b) { return (uint32_t)((a + b - 1) / b); }
