@@ -48,23 +48,30 @@ inline float ord_val(uint32_t k)
 __global__ void __launch_bounds__(256) defect_bounds_kernel(const float4* __restrict__ pos, uint32_t nb,
                                                             uint32_t* __restrict__ box)
 {
-    uint32_t lo_x = 0xffffffffu, lo_y = 0xffffffffu, hi_x = 0u, hi_y = 0u;
+    __shared__ uint32_t s_k[4][8];
+    uint32_t k[4] = {0xffffffffu, 0xffffffffu, 0u, 0u};  // lo x, lo y, hi x, hi y
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += gridDim.x * blockDim.x) {
         const float4 r = pos[i];
         const uint32_t kx = ord_key(r.x), ky = ord_key(r.y);
-        lo_x = min(lo_x, kx), lo_y = min(lo_y, ky), hi_x = max(hi_x, kx), hi_y = max(hi_y, ky);
+        k[0] = min(k[0], kx), k[1] = min(k[1], ky), k[2] = max(k[2], kx), k[3] = max(k[3], ky);
     }
+#pragma unroll
     for (int o = 16; o; o >>= 1) {
-        lo_x = min(lo_x, __shfl_xor_sync(0xffffffffu, lo_x, o));
-        lo_y = min(lo_y, __shfl_xor_sync(0xffffffffu, lo_y, o));
-        hi_x = max(hi_x, __shfl_xor_sync(0xffffffffu, hi_x, o));
-        hi_y = max(hi_y, __shfl_xor_sync(0xffffffffu, hi_y, o));
+        k[0] = min(k[0], __shfl_xor_sync(0xffffffffu, k[0], o));
+        k[1] = min(k[1], __shfl_xor_sync(0xffffffffu, k[1], o));
+        k[2] = max(k[2], __shfl_xor_sync(0xffffffffu, k[2], o));
+        k[3] = max(k[3], __shfl_xor_sync(0xffffffffu, k[3], o));
     }
-    if ((threadIdx.x & 31) == 0) {
-        atomicMin(box + 0, lo_x);
-        atomicMin(box + 1, lo_y);
-        atomicMax(box + 2, hi_x);
-        atomicMax(box + 3, hi_y);
+    const uint32_t w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31u) == 0)
+        for (int a = 0; a < 4; ++a) s_k[a][w] = k[a];
+    __syncthreads();
+    if (threadIdx.x < 4) {  // one atomic per value and block
+        const uint32_t a = threadIdx.x;
+        uint32_t v = s_k[a][0];
+        for (uint32_t q = 1; q < (blockDim.x >> 5); ++q) v = a < 2 ? min(v, s_k[a][q]) : max(v, s_k[a][q]);
+        if (a < 2) atomicMin(box + a, v);
+        else atomicMax(box + a, v);
     }
 }
 
@@ -137,27 +144,29 @@ __global__ void __launch_bounds__(256) defect_circuit_kernel(DefectGrid G, const
 // Touching marked cells (8-neighbourhood, no wrap) of one sign merged; each
 // cluster labelled by its first cell in x-major order, the fixed point of the
 // reference's lowest-neighbour relabelling (analysis/find_defects.py:126-160).
-void cluster(const std::vector<uint32_t>& cells, uint32_t nx, uint32_t ny, std::vector<std::vector<uint32_t>>& out)
+// cells are sorted by x * ny + y, so each cell's earlier neighbours, (x-1, y-1..y+1)
+// and (x, y-1), are found with a pointer that only moves forward.
+void cluster(const std::vector<uint32_t>& cells, uint32_t ny, std::vector<std::vector<uint32_t>>& out)
 {
-    const size_t n = cells.size();  // sorted
+    const size_t n = cells.size();
     std::vector<uint32_t> parent(n);
     for (size_t a = 0; a < n; ++a) parent[a] = (uint32_t)a;
     auto find = [&](uint32_t a) {
         while (parent[a] != a) a = parent[a] = parent[parent[a]];
         return a;
     };
+    auto unite = [&](uint32_t a, uint32_t b) {
+        const uint32_t ra = find(a), rb = find(b);
+        if (ra != rb) parent[std::max(ra, rb)] = std::min(ra, rb);
+    };
+    size_t p = 0;  // first cell at or after (x-1, y-1)
     for (size_t a = 0; a < n; ++a) {
-        const int x = (int)(cells[a] / ny), y = (int)(cells[a] % ny);
-        for (int dx = -1; dx <= 1; ++dx)
-            for (int dy = -1; dy <= 1; ++dy) {
-                const int qx = x + dx, qy = y + dy;
-                if ((dx == 0 && dy == 0) || qx < 0 || qy < 0 || qx >= (int)nx || qy >= (int)ny) continue;
-                const uint32_t q = (uint32_t)qx * ny + (uint32_t)qy;
-                const auto it = std::lower_bound(cells.begin(), cells.end(), q);
-                if (it == cells.end() || *it != q) continue;
-                const uint32_t ra = find((uint32_t)a), rb = find((uint32_t)(it - cells.begin()));
-                if (ra != rb) parent[std::max(ra, rb)] = std::min(ra, rb);
-            }
+        const uint32_t k = cells[a], x = k / ny, y = k % ny;
+        if (a > 0 && y > 0 && cells[a - 1] == k - 1) unite((uint32_t)a, (uint32_t)(a - 1));
+        if (x == 0) continue;
+        const uint32_t lo = (x - 1) * ny + (y > 0 ? y - 1 : 0), hi = (x - 1) * ny + std::min(y + 1, ny - 1);
+        while (p < a && cells[p] < lo) ++p;
+        for (size_t q = p; q < a && cells[q] <= hi; ++q) unite((uint32_t)a, (uint32_t)q);
     }
     std::vector<int> slot(n, -1);
     for (size_t a = 0; a < n; ++a) {
@@ -199,7 +208,7 @@ extern "C" nw_status nw_find_defects(nw_system* s, float cell_size, uint32_t fla
     e = cudaMemsetAsync(box, 0xff, 8, s->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(box + 2, 0, 12, s->stream);
     if (e == cudaSuccess) {
-        defect_bounds_kernel<<<std::min<uint32_t>((s->nb + 255) / 256, 1024), 256, 0, s->stream>>>(pos, s->nb, box);
+        defect_bounds_kernel<<<std::min<uint32_t>((s->nb + 255) / 256, 2 * 152), 256, 0, s->stream>>>(pos, s->nb, box);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(h, box, 16, cudaMemcpyDeviceToHost, s->stream);
@@ -255,7 +264,7 @@ extern "C" nw_status nw_find_defects(nw_system* s, float cell_size, uint32_t fla
         for (uint32_t v : m)
             if ((v & 1u) == (uint32_t)sign) cells.push_back(v >> 1);
         std::vector<std::vector<uint32_t>> clusters;
-        cluster(cells, G.nx, G.ny, clusters);
+        cluster(cells, G.ny, clusters);
         for (const auto& cl : clusters) {
             double mx = 0.0, my = 0.0;
             for (uint32_t c : cl) {

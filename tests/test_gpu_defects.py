@@ -116,3 +116,35 @@ def test_defect_finder_argument_checks(lib):
             with pytest.raises(nwgb.NwError) as e:
                 s.find_defects(bad)
             assert e.value.status == abi.NW_ERR_INVALID
+
+
+def test_defect_finder_edge_cases(lib):
+    """A frame too small for an interior cell has no defects; a short output
+    buffer still reports the full count; non-finite positions are refused;
+    3D systems are not supported."""
+    import ctypes as C
+
+    import nwgb
+
+    with system_with(lib, GOLDEN["pair_c2_pos"][:10], 5) as s:  # two worms: a 3 x 2 grid at most
+        assert len(s.find_defects(2.0)) == 0
+    pos = GOLDEN["isotropic_c2_pos"]
+    want = D.find_defects(pos, 4, 2.0)
+    with system_with(lib, pos, 4) as s:
+        buf = (abi.NwDefect * 1)()
+        n = C.c_int()
+        abi.check(lib.nw_find_defects(s._h, C.c_float(2.0), 0, buf, 1, C.byref(n)))
+        assert n.value == len(want) > 1
+        assert (buf[0].x, buf[0].y, buf[0].charge) == (want["x"][0], want["y"][0], want["charge"][0])
+        assert np.array_equal(rows(s.find_defects(2.0, max_defects=2)), rows(want))  # grows its buffer
+        p = s.get_array(abi.NW_POSITION)
+        p[7, 0] = np.nan
+        s.set_array(abi.NW_POSITION, p)
+        with pytest.raises(nwgb.NwError) as e:
+            s.find_defects(2.0)
+        assert e.value.status == abi.NW_ERR_INVALID
+    cfg3 = abi.default_config(abi.NW_MODEL_WCA_WORMS, 16, 10, (12, 12, 12), False, lib)
+    with nwgb.System(cfg3) as s:
+        with pytest.raises(nwgb.NwError) as e:
+            s.find_defects(2.0)
+        assert e.value.status == abi.NW_ERR_UNSUPPORTED
