@@ -663,6 +663,14 @@ def run_defects(args):
             s.set_array(abi.NW_POSITION, host)
             got = s.find_defects(cs)
         e2e = (time.perf_counter() - t0) / steps
+        # the sampling search (analysis/defects.py defaults: 100 points, radius 10)
+        sample = np.random.default_rng(3).integers(0, nb, 100)
+        for _ in range(3):
+            s.sample_defects(sample, 10.0)
+        t0 = time.perf_counter()
+        for _ in range(20):
+            wind = s.sample_defects(sample, 10.0)
+        sampling_ms = (time.perf_counter() - t0) / 20 * 1e3
     cpu_per, cpu_d = cpu_time(2) if rank == 0 and not args.no_cpu_baseline else (None, None)
     same = cpu_d is None or (len(cpu_d) == len(got) and np.array_equal(cpu_d["x"], got["x"]))
     line = {"metric": "frames/s", "value": 1.0 / per, "unit": "frames/s", "n_gpus": world, "steps": steps,
@@ -671,7 +679,8 @@ def run_defects(args):
             "config": {"workload": args.workload, "beads": nb, "cell_size": cs, "defects": int(len(got))},
             "e2e": {"value": 1.0 / e2e, "unit": "frames/s", "h2d_bytes_per_step": int(pos.nbytes),
                     "d2h_bytes_per_step": int(len(got) * 24 + 4)},
-            "gpu_launches": steps * 3, "matches_cpu": bool(same), "timing": "host wall clock per synchronous call"}
+            "gpu_launches": steps * 3, "matches_cpu": bool(same), "timing": "host wall clock per synchronous call",
+            "sampling": {"points": 100, "radius": 10.0, "ms_per_call": sampling_ms, "kept": int((wind > 0).sum())}}
     if cpu_per is not None:
         line["cpu_baseline"] = {"value": 1.0 / cpu_per, "unit": "frames/s", "cores": 1, "kind": "port",
                                 "sample": "the whole frame, numpy restatement of the reference's analysis"}

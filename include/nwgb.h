@@ -348,6 +348,19 @@ typedef struct NwDefect {
 } NwDefect;
 nw_status nw_find_defects(nw_system* sys, float cell_size, uint32_t flags, NwDefect* out, int max_out, int* n_out);
 
+/* The reference's second, sampling defect search (analysis/defects.py:12-32 with
+ * analysis/afa/utils.py:4-17, 35-54, analysis/afa/data.py:46-52): around each
+ * sample point (the position of bead beads[k]) the beads within `radius`
+ * (plain Euclidean distance, the centre bead included) are binned by the angle of
+ * their displacement from the point into 8 sectors of pi/4 from -pi; a sector's
+ * director is the angle of its beads' mean tangent (tangents as in
+ * nw_find_defects); winding[k] = round(sum of the differences of the sector
+ * directors / pi) over sectors 0 .. the highest occupied one (empty sectors read
+ * 0), in float64.  The reference keeps the points with winding > 0.  One block
+ * per sample point, fixed-order sums.  Synchronous.  2D systems. */
+nw_status nw_sample_defects(nw_system* sys, const uint32_t* beads, int n_points, float radius, uint32_t flags,
+                            int32_t* winding);
+
 /* Numerics self-check of the refined reciprocal, square root and quotient
  * the force laws use (no reference counterpart).  For host arrays a[n] and
  * b[n] of positive normal floats it writes, per element, out[4*i + 0..3] =

@@ -181,6 +181,90 @@ void cluster(const std::vector<uint32_t>& cells, uint32_t ny, std::vector<std::v
 
 }  // namespace
 
+// ---- the sampling search (analysis/defects.py) ------------------------------
+
+constexpr int kSectors = 8;
+
+// Unit tangent of bead i in float64 (analysis/afa/utils.py:35-49): zero for
+// the first and the last bead of the system and for coincident neighbours.
+__device__ __forceinline__ void tangent64(const nw::DevParams& P, const float4* __restrict__ pos, uint32_t i,
+                                          bool min_image, double& tx, double& ty)
+{
+    tx = ty = 0.0;
+    if (i == 0 || i + 1 >= P.nb) return;
+    const uint32_t c = i % P.L;
+    const uint32_t a = c == 0 ? i : i - 1, b = c + 1 == P.L ? i : i + 1;
+    const float4 pa = pos[a], pb = pos[b];
+    double dx, dy, dz;
+    if (min_image) {
+        float3 d = make_float3(pb.x - pa.x, pb.y - pa.y, pb.z - pa.z);
+        nw::min_image(P, d);
+        dx = d.x, dy = d.y, dz = d.z;
+    } else {
+        dx = (double)pb.x - (double)pa.x, dy = (double)pb.y - (double)pa.y, dz = (double)pb.z - (double)pa.z;
+    }
+    const double nrm = sqrt(dx * dx + dy * dy + dz * dz);
+    if (nrm > 0.0) tx = dx / nrm, ty = dy / nrm;
+}
+
+// One block per sample point: per-sector sums of the tangents of the beads
+// within the radius, combined in a fixed order, then the winding value.
+__global__ void __launch_bounds__(256) sample_defect_kernel(const nw::DevParams P, const float4* __restrict__ pos,
+                                                            const uint32_t* __restrict__ beads, double r2,
+                                                            bool min_image, int32_t* __restrict__ winding)
+{
+    __shared__ double s_x[kSectors][8], s_y[kSectors][8];
+    __shared__ uint32_t s_n[kSectors][8];
+    const uint32_t centre = beads[blockIdx.x];
+    const float4 c4 = pos[centre];
+    const double cx = c4.x, cy = c4.y;
+    const double w = 2.0 * 3.141592653589793 / 8.0;  // BIN_EDGES[8] of analysis/afa/utils.py:8-11
+    double sx[kSectors], sy[kSectors];
+    uint32_t sn[kSectors];
+#pragma unroll
+    for (int k = 0; k < kSectors; ++k) sx[k] = sy[k] = 0.0, sn[k] = 0u;
+    for (uint32_t i = threadIdx.x; i < P.nb; i += blockDim.x) {
+        const float4 r = pos[i];
+        const double dx = (double)r.x - cx, dy = (double)r.y - cy;
+        if (!(dx * dx + dy * dy <= r2)) continue;
+        const double ang = atan2(dy, dx);
+        int bin = -1;  // np.digitize(angle, edges) - 1: edges at or below the angle, less one
+#pragma unroll
+        for (int k = 0; k < kSectors; ++k) bin += (double)(k - 4) * w <= ang ? 1 : 0;
+        double tx, ty;
+        tangent64(P, pos, i, min_image, tx, ty);
+#pragma unroll
+        for (int k = 0; k < kSectors; ++k)
+            if (k == bin) sx[k] += tx, sy[k] += ty, ++sn[k];
+    }
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < kSectors; ++k) {
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            sx[k] += __shfl_down_sync(0xffffffffu, sx[k], o);
+            sy[k] += __shfl_down_sync(0xffffffffu, sy[k], o);
+            sn[k] += __shfl_down_sync(0xffffffffu, sn[k], o);
+        }
+        if (lane == 0) s_x[k][wid] = sx[k], s_y[k][wid] = sy[k], s_n[k][wid] = sn[k];
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    double ang[kSectors];
+    int top = -1;
+    for (int k = 0; k < kSectors; ++k) {
+        double X = 0.0, Y = 0.0;
+        uint32_t n = 0;
+        for (uint32_t q = 0; q < (blockDim.x >> 5); ++q) X += s_x[k][q], Y += s_y[k][q], n += s_n[k][q];
+        ang[k] = n ? atan2(Y / (double)n, X / (double)n) : 0.0;  // compute_director_angle of the mean
+        if (n) top = k;
+    }
+    // winding_number(director_angles, pi) = round(sum(diff(angles / pi)))
+    double sum = 0.0;
+    for (int k = 0; k < top; ++k) sum += ang[k + 1] / 3.141592653589793 - ang[k] / 3.141592653589793;
+    winding[blockIdx.x] = (int32_t)rint(sum);
+}
+
 // Fixed workspace: 8 words of bounds and counters, then the marked cells.
 constexpr uint32_t kMarkCap = 1u << 16;  // marked cells reported (defects are rare)
 constexpr uint32_t kMarkFirst = 4096;    // marked cells copied back with the count
@@ -278,5 +362,39 @@ extern "C" nw_status nw_find_defects(nw_system* s, float cell_size, uint32_t fla
         }
     }
     *n_out = n;
+    return NW_OK;
+}
+
+extern "C" nw_status nw_sample_defects(nw_system* s, const uint32_t* beads, int n_points, float radius,
+                                       uint32_t flags, int32_t* winding)
+{
+    if (!s || n_points < 0 || (n_points > 0 && (!beads || !winding))) return NW_ERR_INVALID;
+    if (!(radius >= 0.f) || !std::isfinite(radius) || (flags & ~NW_DEFECT_MIN_IMAGE)) return NW_ERR_INVALID;
+    if (s->cfg.dim >= 3) return NW_ERR_UNSUPPORTED;
+    if (n_points == 0) return NW_OK;
+    for (int k = 0; k < n_points; ++k)
+        if (beads[k] >= s->nb) return NW_ERR_INVALID;
+    const float4* pos = s->B.pos2[s->lists ? (uint32_t)((s->step + 1ull) & 1ull) : 0u];
+    uint32_t* d_beads = nullptr;
+    int32_t* d_w = nullptr;
+    cudaError_t e = cudaMalloc(&d_beads, (size_t)n_points * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&d_w, (size_t)n_points * 4);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_beads, beads, (size_t)n_points * 4, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) {
+        const nw::DevParams P = nw::make_dev_params(s->cfg, s->cfg.dt);
+        const double r = (double)radius;
+        sample_defect_kernel<<<(uint32_t)n_points, 256, 0, s->stream>>>(P, pos, d_beads, r * r,
+                                                                         (flags & NW_DEFECT_MIN_IMAGE) != 0, d_w);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(winding, d_w, (size_t)n_points * 4, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(d_beads);
+    cudaFree(d_w);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? NW_ERR_NOMEM : NW_ERR_CUDA;
+    }
     return NW_OK;
 }

@@ -222,6 +222,7 @@ HANDLE_API = [
     ("nw_writer_flush", C.c_int, [_P]),
     ("nw_writer_close", C.c_int, [_P]),
     ("nw_find_defects", C.c_int, [_sysp, _f32, _u32, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    ("nw_sample_defects", C.c_int, [_sysp, C.c_void_p, C.c_int, _f32, _u32, C.c_void_p]),
 ]
 
 _fp = C.c_void_p  # device pointers are passed as integers

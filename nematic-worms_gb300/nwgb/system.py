@@ -169,6 +169,18 @@ class System:
             return self.find_defects(cell_size, min_image, n.value)
         return np.frombuffer(buf, dtype=abi.DEFECT_DTYPE, count=n.value).copy()
 
+    def sample_defects(self, beads, radius: float = 10.0, min_image: bool = False) -> np.ndarray:
+        """Winding value around the position of each bead in `beads`
+        (analysis/defects.py:12-32 on the device); the reference keeps the
+        sample points whose value is positive.  `beads` are the sample bead
+        indices (the reference draws them with np.random.randint)."""
+        idx = np.ascontiguousarray(np.asarray(beads, dtype=np.uint32).reshape(-1))
+        out = np.zeros(idx.shape[0], dtype=np.int32)
+        flags = abi.NW_DEFECT_MIN_IMAGE if min_image else 0
+        check(self.lib.nw_sample_defects(self._h, idx.ctypes.data, int(idx.shape[0]), float(radius), flags,
+                                         out.ctypes.data), "nw_sample_defects")
+        return out
+
     # -- checkpoints ------------------------------------------------------------------------
     def checkpoint(self) -> bytes:
         n = C.c_size_t()

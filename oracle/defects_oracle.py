@@ -141,3 +141,28 @@ def find_defects(pos: np.ndarray, filament_length: int, cell_size: float = 2.0, 
         for ci, cj, cnt in _cluster(marked & (np.sign(total) == sign)):
             rows.append((ci * cell_size + centre[0], cj * cell_size + centre[1], charge, cnt))
     return np.array(rows, dtype=[("x", "f8"), ("y", "f8"), ("charge", "f4"), ("cells", "u4")])
+
+
+def sample_windings(pos: np.ndarray, filament_length: int, beads, radius: float = 10.0, box=None) -> np.ndarray:
+    """Winding value around each sample bead's position, the sampling search of
+    analysis/defects.py:12-32 (with analysis/afa/utils.py:4-17, 35-54): beads
+    within `radius` (Euclidean, the centre included) binned into 8 sectors of
+    pi/4 from -pi by np.digitize of their displacement angle, a sector's
+    director the angle of its mean tangent, then round(sum(diff(angles / pi)))
+    over sectors 0 .. the highest occupied (empty sectors read 0)."""
+    r = np.asarray(pos, dtype=np.float64)[:, :2]
+    t = tangents(pos, filament_length, box)
+    edges = [(i - 4) * (2 * np.pi / 8) for i in range(8)]
+    out = np.zeros(len(beads), dtype=np.int32)
+    for k, b in enumerate(np.asarray(beads)):
+        d = r - r[b]
+        near = np.nonzero(d[:, 0] ** 2 + d[:, 1] ** 2 <= radius * radius)[0]
+        sector = np.digitize(np.arctan2(d[near, 1], d[near, 0]), edges) - 1
+        ids = np.unique(sector)
+        angles = np.zeros(ids.max() + 1)
+        for s_ in ids:
+            m = t[near[sector == s_]].mean(axis=0)
+            angles[s_] = np.arctan2(m[1], m[0])
+        out[k] = round(np.sum(np.diff(angles / np.pi)))
+    return out
+

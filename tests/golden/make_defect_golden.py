@@ -6,7 +6,8 @@ Runs the reference's Python functions in place (read-only checkout given by
 director field handed to analysis/find_defects.py compute_theta and
 find_defects as read_vector_field would hand it over (the y component of the
 director negated, as make_director_field.py:79 writes it), without the text
-round trip.  The reference's code uses the ``np.int`` alias that numpy 2
+round trip; and analysis/defects.py search_for_defects, the sampling search,
+on four of the frames.  The reference's code uses the ``np.int`` alias that numpy 2
 removed; it is put back as ``int`` for the run.
 
 Frames are translated so that the lowest bead sits at (1, 1) exactly: the
@@ -152,6 +153,28 @@ def reference_defects(ref_analysis: Path, pos: np.ndarray, L: int, cellsize: flo
     return np.array([(x, y, q) for (_, x, y, _, q) in out], dtype=np.float64).reshape(-1, 3)
 
 
+def reference_sampling(ref_analysis: Path, pos: np.ndarray, L: int, n_points: int, radius: float, seed: int):
+    """The reference's sampling search, analysis/defects.py search_for_defects,
+    called as its __main__ does (neighbour tree and tangents built first) with
+    numpy's global generator seeded; the sample bead indices are the draw it
+    makes (afa/data.py sample_points), repeated from the same seed.  Returns the
+    indices and the kept points' values (winding > 0) in draw order."""
+    sys.path.insert(0, str(ref_analysis))
+    from afa.data import Frame
+    from defects import search_for_defects
+
+    r = pos.astype(np.float64)
+    frame = Frame(positions=r, labels=np.zeros(len(r)), filament_length=L)
+    frame.build_neighbors_list()
+    frame.compute_filament_tangents()
+    np.random.seed(seed)
+    dc = search_for_defects(frame, {"radius": radius, "n_points": n_points})
+    np.random.seed(seed)
+    beads = np.random.randint(0, len(frame), size=n_points).astype(np.uint32)
+    kept = np.array([[p[0], p[1], v] for p, v in zip(dc.r, dc.v)], dtype=np.float64).reshape(-1, 3)
+    return beads, kept
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", required=True, help="checkout of the reference project")
@@ -177,6 +200,11 @@ def main():
         arrays[f"{name}_defects"] = d
         print(f"{name}: {len(pos)} beads, L={L}, cellsize={cs}: {len(d)} defects "
               f"(+{int((d[:, 2] > 0).sum())} / -{int((d[:, 2] < 0).sum())})")
+        if name in ("pair_c2", "quad_c3", "isotropic_c2", "junction_c2"):
+            beads, kept = reference_sampling(ana, pos, L, 200, 6.0, seed=len(pos))
+            arrays[f"{name}_sample_beads"] = beads
+            arrays[f"{name}_sample_kept"] = kept
+            print(f"  sampling search: 200 points, radius 6: {len(kept)} kept")
     np.savez_compressed(HERE / "defects_2d.npz", **arrays)
 
 

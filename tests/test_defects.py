@@ -80,3 +80,25 @@ def test_tangents_follow_the_reference_window():
     assert np.all(t[0] == 0) and np.all(t[-1] == 0)  # no window is centred on the first or last bead
     assert np.allclose(t[1], [1, 0]) and np.allclose(t[2], [1, 0])  # one-sided at the filament tail
     assert np.allclose(t[3], [0, 1]) and np.allclose(t[4], [0, 1])
+
+
+SAMPLED = sorted(k[: -len("_sample_beads")] for k in GOLDEN.files if k.endswith("_sample_beads"))
+
+
+@pytest.mark.parametrize("name", SAMPLED)
+def test_sampling_oracle_matches_reference(name):
+    """The sampling search (analysis/defects.py search_for_defects, run by the
+    golden script with its draw seeded): the same kept points and values."""
+    pos = GOLDEN[name + "_pos"]
+    L, _ = GOLDEN[name + "_meta"]
+    beads = GOLDEN[name + "_sample_beads"]
+    kept = GOLDEN[name + "_sample_kept"]
+    w = D.sample_windings(pos, int(L), beads, 6.0)
+    sel = w > 0
+    got = np.stack([pos[beads[sel], 0].astype(np.float64), pos[beads[sel], 1].astype(np.float64),
+                    w[sel].astype(np.float64)], 1)
+    assert np.array_equal(got, kept)
+
+
+def test_sampling_golden_frames_keep_points():
+    assert sum(len(GOLDEN[n + "_sample_kept"]) for n in SAMPLED) > 20

@@ -148,3 +148,33 @@ def test_defect_finder_edge_cases(lib):
         with pytest.raises(nwgb.NwError) as e:
             s.find_defects(2.0)
         assert e.value.status == abi.NW_ERR_UNSUPPORTED
+
+
+SAMPLED = sorted(k[: -len("_sample_beads")] for k in GOLDEN.files if k.endswith("_sample_beads"))
+
+
+@pytest.mark.parametrize("name", SAMPLED)
+def test_device_sampling_search_matches_reference(lib, name):
+    pos = GOLDEN[name + "_pos"]
+    L, _ = GOLDEN[name + "_meta"]
+    beads = GOLDEN[name + "_sample_beads"]
+    with system_with(lib, pos, int(L)) as s:
+        w = s.sample_defects(beads, 6.0)
+    assert np.array_equal(w, D.sample_windings(pos, int(L), beads, 6.0))
+    sel = w > 0
+    got = np.stack([pos[beads[sel], 0].astype(np.float64), pos[beads[sel], 1].astype(np.float64),
+                    w[sel].astype(np.float64)], 1)
+    assert np.array_equal(got, GOLDEN[name + "_sample_kept"])
+
+
+def test_device_sampling_search_on_a_large_frame(lib):
+    rng = np.random.default_rng(12)
+    pos = planted_frame(rng, 20000, 10, 400.0, [(120, 200, 0.5), (280, 200, -0.5)], jitter=0.4)
+    beads = rng.integers(0, len(pos), 300)
+    with system_with(lib, pos, 10) as s:
+        w = s.sample_defects(beads, 10.0)
+        with pytest.raises(Exception):
+            s.sample_defects([len(pos)], 10.0)  # bead index out of range
+    want = D.sample_windings(pos, 10, beads, 10.0)
+    assert (want != 0).any()
+    assert np.array_equal(w, want)
