@@ -228,6 +228,21 @@ def config_block(name, cfg, world):
             "l2": "state larger than L2 (no flush needed)"}
 
 
+def job_rate(dist, ms_local: float, units_local: float, device="cpu"):
+    """Whole-job throughput over the ranks: the units all ranks processed
+    divided by the slowest rank's time (max over ranks).  Returns
+    (units per second, max ms)."""
+    import torch
+
+    t_ms = torch.tensor([ms_local], dtype=torch.float64, device=device)
+    t_units = torch.tensor([units_local], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t_ms, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t_units, op=dist.ReduceOp.SUM)
+    ms_max = float(t_ms.item())
+    return float(t_units.item()) / (ms_max / 1e3), ms_max
+
+
 def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
@@ -329,11 +344,7 @@ def run_ours(args):
     if dist:
         dist.barrier()
     sysm.sync()
-    ms_t = torch.tensor([ms], device="cuda")
-    if dist:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms_max = float(ms_t.item())
-    value = nb * args.steps * world / (ms_max / 1e3)
+    value, ms_max = job_rate(dist, ms, nb * args.steps, device="cuda")
 
     # ---- end to end through the C ABI with host buffers ------------------------------
     e2e_steps = max(chunk, min(200, args.steps))
@@ -358,10 +369,7 @@ def run_ours(args):
     for _ in range(e2e_steps):
         e2e_step()
     e2e_s = time.perf_counter() - t0
-    e2e_t = torch.tensor([e2e_s], device="cuda")
-    if dist:
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_value = nb * e2e_steps * world / float(e2e_t.item())
+    e2e_value, _ = job_rate(dist, 1e3 * e2e_s, nb * e2e_steps, device="cuda")
 
     # ---- per-kernel device time (events around every launch) ---------------------------
     prof = sysm.profile(2 * chunk, cfg.dt)
