@@ -385,13 +385,21 @@ __device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& 
         }
         __syncthreads();
     }
+    // largest displacement of update n (float bits order like the values): a
+    // warp maximum, then one atomic per block (one per warp on a single word
+    // serialises in L2 and cost 1.4 us of a 26 us step kernel)
+    __shared__ uint32_t s_dmax[32];
     if (P.vl_on) {
-        // largest displacement of update n (float bits order like the values)
         const uint32_t m = __reduce_max_sync(0xffffffffu, __float_as_uint(disp2));
-        if ((t & 31u) == 0u && m) atomicMax(&S.vstate[2u + (uint32_t)(n % 3ull)], __float_as_uint(sqrtf(__uint_as_float(m))));
+        if ((t & 31u) == 0u) s_dmax[t >> 5] = m;
     }
     if (active) smp[t] = nP;
     __syncthreads();
+    if (P.vl_on && t == 0) {
+        uint32_t m = 0u;
+        for (uint32_t q = 0; q < (blockDim.x + 31u) >> 5; ++q) m = s_dmax[q] > m ? s_dmax[q] : m;
+        if (m) atomicMax(&S.vstate[2u + (uint32_t)(n % 3ull)], __float_as_uint(sqrtf(__uint_as_float(m))));
+    }
     const uint32_t wl = active ? t / L : 0u, c = active ? t - wl * L : 0u;
     const float4* R = smp + wl * L;
     // each bending triple once, by the thread of its first bead
