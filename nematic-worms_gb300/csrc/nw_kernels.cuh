@@ -58,8 +58,8 @@ struct StepBuffers {
     uint32_t *srd_bcount, *srd_scount, *srd_boff, *srd_soff, *srd_bchunk, *srd_schunk;
     uint32_t *srd_start, *srd_end;
     float4* srd_mean;
-    // SRD cells of warps holding more members than the warp path stages,
-    // handed to srd_collide_big_kernel: srd_big[0 .. *srd_nbig)
+    // SRD cells of more than kLaneCap members, handed to
+    // srd_collide_big_kernel: srd_big[0 .. *srd_nbig)
     uint32_t *srd_big, *srd_nbig;
     uint32_t* err;
     unsigned long long* step_base;
@@ -547,12 +547,12 @@ __global__ void __launch_bounds__(256) srd_hash_kernel(const DevParams P, const 
 // mass-weighted cell mean (:560-594), the +/- alpha rotation of (v - u)
 // (:640-691), the relative-velocity thermostat when selected, and the
 // solvent's ballistic streaming by dt_srd (solvent_integrator, :145-205).
-__global__ void __launch_bounds__(128) srd_collide_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
-                                                          float dt_srd, uint32_t buf_sel);
+__global__ void __launch_bounds__(128, 8) srd_collide_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
+                                                             float dt_srd, uint32_t buf_sel);
 
 __global__ void __launch_bounds__(256) srd_scatter_kernel(const DevParams P, const StepBuffers S);
 // One warp per SRD cell of the srd_big list (grid-stride over the list).
-__global__ void __launch_bounds__(256) srd_collide_big_kernel(const DevParams P, const StepBuffers S,
+__global__ void __launch_bounds__(128) srd_collide_big_kernel(const DevParams P, const StepBuffers S,
                                                               uint32_t step_off, float dt_srd, uint32_t buf_sel);
 constexpr uint32_t kSrdBigBlocks = 608;  // 4 blocks per SM
 constexpr uint32_t kLaneCap = 16;        // members of a cell collided by one lane of srd_collide_kernel
