@@ -375,10 +375,18 @@ extern "C" nw_status nw_sample_defects(nw_system* s, const uint32_t* beads, int 
     for (int k = 0; k < n_points; ++k)
         if (beads[k] >= s->nb) return NW_ERR_INVALID;
     const float4* pos = s->B.pos2[s->lists ? (uint32_t)((s->step + 1ull) & 1ull) : 0u];
+    // the system's defect workspace holds up to kMarkCap / 2 points; more take their own
     uint32_t* d_beads = nullptr;
     int32_t* d_w = nullptr;
-    cudaError_t e = cudaMalloc(&d_beads, (size_t)n_points * 4);
-    if (e == cudaSuccess) e = cudaMalloc(&d_w, (size_t)n_points * 4);
+    const bool own = (uint32_t)n_points > kMarkCap / 2u;
+    cudaError_t e = cudaSuccess;
+    if (!own && !s->defect_fixed) e = cudaMalloc(&s->defect_fixed, 32 + (size_t)kMarkCap * 4);
+    if (e == cudaSuccess && !own) {
+        d_beads = (uint32_t*)s->defect_fixed + 8;
+        d_w = (int32_t*)(d_beads + n_points);
+    }
+    if (e == cudaSuccess && own) e = cudaMalloc(&d_beads, (size_t)n_points * 4);
+    if (e == cudaSuccess && own) e = cudaMalloc(&d_w, (size_t)n_points * 4);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d_beads, beads, (size_t)n_points * 4, cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) {
@@ -390,8 +398,10 @@ extern "C" nw_status nw_sample_defects(nw_system* s, const uint32_t* beads, int 
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(winding, d_w, (size_t)n_points * 4, cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    cudaFree(d_beads);
-    cudaFree(d_w);
+    if (own) {
+        cudaFree(d_beads);
+        cudaFree(d_w);
+    }
     if (e != cudaSuccess) {
         cudaGetLastError();
         return e == cudaErrorMemoryAllocation ? NW_ERR_NOMEM : NW_ERR_CUDA;

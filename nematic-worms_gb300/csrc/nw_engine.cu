@@ -221,12 +221,14 @@ __global__ void __launch_bounds__(256) set_positions_kernel(const float4* __rest
         m = bits > m ? bits : m;
         dst[i] = a;
     }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        const uint32_t t = __shfl_xor_sync(0xffffffffu, m, o);
-        m = t > m ? t : m;
+    __shared__ uint32_t s_m[8];
+    m = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31u) == 0u) s_m[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {  // one atomic per block on the shared word
+        for (uint32_t q = 1; q < (blockDim.x >> 5); ++q) m = s_m[q] > m ? s_m[q] : m;
+        if (m) atomicMax(dmax, m);
     }
-    if ((threadIdx.x & 31u) == 0u && m) atomicMax(dmax, m);
 }
 
 __global__ void vl_add_displacement_kernel(uint32_t* __restrict__ vstate, uint32_t slot)
