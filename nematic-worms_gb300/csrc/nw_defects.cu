@@ -146,7 +146,12 @@ __global__ void __launch_bounds__(256) defect_circuit_kernel(DefectGrid G, const
 // reference's lowest-neighbour relabelling (analysis/find_defects.py:126-160).
 // cells are sorted by x * ny + y, so each cell's earlier neighbours, (x-1, y-1..y+1)
 // and (x, y-1), are found with a pointer that only moves forward.
-void cluster(const std::vector<uint32_t>& cells, uint32_t ny, std::vector<std::vector<uint32_t>>& out)
+struct Cluster {
+    double sx, sy;  // sums of the member cells' x and y indices
+    uint32_t n;     // member cells
+};
+
+void cluster(const std::vector<uint32_t>& cells, uint32_t ny, std::vector<Cluster>& out)
 {
     const size_t n = cells.size();
     std::vector<uint32_t> parent(n);
@@ -168,14 +173,19 @@ void cluster(const std::vector<uint32_t>& cells, uint32_t ny, std::vector<std::v
         while (p < a && cells[p] < lo) ++p;
         for (size_t q = p; q < a && cells[q] <= hi; ++q) unite((uint32_t)a, (uint32_t)q);
     }
+    // clusters in order of their first cell (each root is its cluster's lowest
+    // index); member index sums in cell order, exact in double
     std::vector<int> slot(n, -1);
     for (size_t a = 0; a < n; ++a) {
         const uint32_t r = find((uint32_t)a);
         if (slot[r] < 0) {
             slot[r] = (int)out.size();
-            out.emplace_back();
+            out.push_back(Cluster{0.0, 0.0, 0u});
         }
-        out[slot[r]].push_back(cells[a]);
+        Cluster& c = out[slot[r]];
+        c.sx += (double)(cells[a] / ny);
+        c.sy += (double)(cells[a] % ny);
+        ++c.n;
     }
 }
 
@@ -347,17 +357,11 @@ extern "C" nw_status nw_find_defects(nw_system* s, float cell_size, uint32_t fla
         std::vector<uint32_t> cells;
         for (uint32_t v : m)
             if ((v & 1u) == (uint32_t)sign) cells.push_back(v >> 1);
-        std::vector<std::vector<uint32_t>> clusters;
+        std::vector<Cluster> clusters;
         cluster(cells, G.ny, clusters);
-        for (const auto& cl : clusters) {
-            double mx = 0.0, my = 0.0;
-            for (uint32_t c : cl) {
-                mx += (double)(c / G.ny);
-                my += (double)(c % G.ny);
-            }
-            mx /= (double)cl.size();
-            my /= (double)cl.size();
-            if (n < max_out) out[n] = NwDefect{mx * G.cs + ox, my * G.cs + oy, sign ? 0.5f : -0.5f, (uint32_t)cl.size()};
+        for (const Cluster& cl : clusters) {
+            const double mx = cl.sx / (double)cl.n, my = cl.sy / (double)cl.n;
+            if (n < max_out) out[n] = NwDefect{mx * G.cs + ox, my * G.cs + oy, sign ? 0.5f : -0.5f, cl.n};
             ++n;
         }
     }
