@@ -288,8 +288,9 @@ __global__ void __launch_bounds__(256) srd_scatter_kernel(const DevParams P, con
 // contiguous range of the new solvent storage.  So the warp gathers the
 // members' velocities and positions lane-strided into shared memory (the
 // previous collision's cell order keeps them in a compact region), each
-// thread collides its own cell from shared memory, and the warp writes the
-// stable order and the streamed solvent back coalesced.
+// thread takes its own cell's sums from shared memory, every lane then
+// updates the members of its slots, and the warp writes the stable order and
+// the streamed solvent back coalesced.
 //
 // Per cell, in the member order (the cell's beads, then its solvent, each by
 // index): the reference's isokinetic scaling (particles_kernel_impl.cuh:605-637)
@@ -415,12 +416,16 @@ __global__ void __launch_bounds__(kCollideWarps * 32, 8) srd_collide_kernel(cons
             }
         }
         __syncwarp();
+        // per cell, by its lane: [lab isokinetic factor], mean velocity, rotation
+        // sign, [relative-velocity thermostat factor]
+        const bool lab = P.srd_thermo == NW_SRD_THERMO_REF_LAB;
+        const float ca = P.srd_cos_a;
         float3 u = zero3();
+        float lam1 = 1.0f, sa = 0.0f, lam2 = 1.0f;
+        bool scale2 = false;
         if (mine && n > 0) {
-            uint32_t* ids = &s_id[w][loc - base];
-            float4* V_ = &s_v[w][loc - base];
-            float4* P_ = &s_p[w][loc - base];
-            const bool lab = P.srd_thermo == NW_SRD_THERMO_REF_LAB;
+            const uint32_t* ids = &s_id[w][loc - base];
+            const float4* V_ = &s_v[w][loc - base];
             float E = 0.f;
             if (lab)
                 for (uint32_t k = 0; k < n; ++k) {
@@ -429,12 +434,11 @@ __global__ void __launch_bounds__(kCollideWarps * 32, 8) srd_collide_kernel(cons
                     E += (0.5f * V.w) * dot3(v, v);
                 }
             // reference isokinetic rule: lambda scales every member before the mean
-            const float lam1 = lab ? sqrtf(P.srd_kT / E) : 1.0f;
-            auto scaled = [&](float4 V) -> float3 { return lab ? make_float3(lam1 * V.x, lam1 * V.y, lam1 * V.z) : f3(V); };
+            lam1 = lab ? sqrtf(P.srd_kT / E) : 1.0f;
             float M = 0.f;
             for (uint32_t k = 0; k < n; ++k) {
                 const float4 V = V_[k];
-                u += V.w * scaled(V);
+                u += V.w * (lab ? make_float3(lam1 * V.x, lam1 * V.y, lam1 * V.z) : f3(V));
                 M += V.w;
             }
             if (M > 0.f) {
@@ -443,16 +447,14 @@ __global__ void __launch_bounds__(kCollideWarps * 32, 8) srd_collide_kernel(cons
             }
             // rotation by +alpha or -alpha with equal probability
             const bool plus = u01(rng_draw(P, c, step, kRngSrdRot).x) > 0.5f;
-            const float sa = plus ? P.srd_sin_a : -P.srd_sin_a, ca = P.srd_cos_a;
-            float lam2 = 1.0f;
-            bool scale2 = false;
+            sa = plus ? P.srd_sin_a : -P.srd_sin_a;
             if (P.srd_thermo == NW_SRD_THERMO_CELL_REL) {
                 uint32_t nrot = 0;
                 float ke = 0.f;
                 for (uint32_t k = 0; k < n; ++k) {
                     if (ids[k] < P.nb && !P.srd_rotate_beads) continue;
                     const float4 V = V_[k];
-                    const float3 d = scaled(V) - u;
+                    const float3 d = (lab ? make_float3(lam1 * V.x, lam1 * V.y, lam1 * V.z) : f3(V)) - u;
                     const float rx = d.x * ca - d.y * sa;
                     const float ry = d.x * sa + d.y * ca;
                     ke += (0.5f * V.w) * (rx * rx + ry * ry);
@@ -463,32 +465,52 @@ __global__ void __launch_bounds__(kCollideWarps * 32, 8) srd_collide_kernel(cons
                     scale2 = true;
                 }
             }
-            for (uint32_t k = 0; k < n; ++k) {
-                const uint32_t id = ids[k];
+        }
+        // every member updated by the lane of its slot (the cell's factors from
+        // the cell's lane): rotation, thermostat, solvent streaming, and the
+        // member's destination in the new solvent storage (beads: none)
+        __syncwarp();
+        for (uint32_t j0 = 0; j0 < rtotal; j0 += 32u) {
+            const uint32_t j = j0 + lane, slot = base + (j < rtotal ? j : 0u);
+            uint32_t q = 0;  // the cell of slot, as above
+#pragma unroll
+            for (uint32_t st = 16; st; st >>= 1) {
+                const uint32_t lq = __shfl_sync(0xffffffffu, loc, (int)(q + st));
+                if (lq <= slot) q += st;
+            }
+            const float3 uq = make_float3(__shfl_sync(0xffffffffu, u.x, (int)q), __shfl_sync(0xffffffffu, u.y, (int)q),
+                                          __shfl_sync(0xffffffffu, u.z, (int)q));
+            const float l1 = __shfl_sync(0xffffffffu, lam1, (int)q), saq = __shfl_sync(0xffffffffu, sa, (int)q);
+            const float l2 = __shfl_sync(0xffffffffu, lam2, (int)q);
+            const bool sc2 = __shfl_sync(0xffffffffu, (int)scale2, (int)q) != 0;
+            const uint32_t lq = __shfl_sync(0xffffffffu, loc, (int)q), nq = __shfl_sync(0xffffffffu, nbc, (int)q);
+            const uint32_t sq = __shfl_sync(0xffffffffu, s0, (int)q);
+            if (j < rtotal) {
+                const uint32_t id = s_id[w][j], k = slot - lq;
                 const bool is_bead = id < P.nb;
-                const float4 V = V_[k];
-                float3 v = scaled(V);
+                const float4 V = s_v[w][j];
+                float3 v = lab ? make_float3(l1 * V.x, l1 * V.y, l1 * V.z) : f3(V);
                 if (!is_bead || P.srd_rotate_beads) {
-                    const float3 d = v - u;
-                    const float rx = d.x * ca - d.y * sa;
-                    const float ry = d.x * sa + d.y * ca;
-                    v = make_float3(u.x + rx, u.y + ry, u.z + d.z);
-                    if (scale2) v = make_float3(u.x + lam2 * (v.x - u.x), u.y + lam2 * (v.y - u.y), v.z);
+                    const float3 d = v - uq;
+                    const float rx = d.x * ca - d.y * saq;
+                    const float ry = d.x * saq + d.y * ca;
+                    v = make_float3(uq.x + rx, uq.y + ry, uq.z + d.z);
+                    if (sc2) v = make_float3(uq.x + l2 * (v.x - uq.x), uq.y + l2 * (v.y - uq.y), v.z);
                 }
                 if (is_bead) {
                     if (lab || P.srd_rotate_beads) bvel[id] = make_float4(v.x, v.y, v.z, V.w);
+                    s_id[w][j] = kEmpty;
                 } else {
-                    const float4 P4 = P_[k];
+                    const float4 P4 = s_p[w][j];
                     float3 p = f3(P4);
                     const float3 dr = dt_srd * v;
                     p += dr;
                     apply_boundaries(P, p, v, dr, 0.0f);
-                    P_[k] = make_float4(p.x, p.y, p.z, P4.w);
-                    V_[k] = make_float4(v.x, v.y, v.z, V.w);
+                    s_p[w][j] = make_float4(p.x, p.y, p.z, P4.w);
+                    s_v[w][j] = make_float4(v.x, v.y, v.z, V.w);
+                    s_id[w][j] = sq + (k - nq);
                 }
             }
-            // destinations in the new solvent storage (beads: none)
-            for (uint32_t k = 0; k < n; ++k) ids[k] = k < nbc ? kEmpty : s0 + (k - nbc);
         }
         if (mine && valid && !big) S.srd_mean[c] = make_float4(u.x, u.y, u.z, 0.f);
         __syncwarp();
