@@ -95,3 +95,23 @@ def test_large_move_rebuilds_the_lists(lib):
         pa, va = state(a)
         pb, vb = state(b)
     assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+
+
+def test_tangents_read_through_the_device_pointer_are_current(lib):
+    """WCA worms' steps store no tangents; asking for the device array computes
+    them, so a caller reading the raw pointer (as the reference's host code does
+    with copyArrayFromDevice) sees the tangents of the current positions."""
+    import ctypes as C
+
+    cfg, s = verlet_system(lib)
+    with s:
+        s.step(7, cfg.dt)
+        want = s.get_array(abi.NW_TANGENT)
+        s.step(5, cfg.dt)
+        ptr = s.device_ptr(abi.NW_TANGENT)
+        raw = np.zeros((cfg.n_beads, 4), dtype=np.float32)
+        lib.copyArrayFromDevice(raw.ctypes.data, C.c_void_p(ptr), None, raw.nbytes)
+        now = s.get_array(abi.NW_TANGENT)
+    assert np.array_equal(raw, now)
+    assert not np.array_equal(now, want)  # the worms moved between the two reads
+    assert np.allclose(np.linalg.norm(now[:, :2], axis=1), 1.0, atol=1e-5)
