@@ -1,7 +1,10 @@
 // nw_defects.cu — +1/2 / -1/2 defects of the director field on the device
-// (include/nwgb.h, "topological defects").
+// (include/nwgb.h, "topological defects"): the grid search of
+// analysis/find_defects.py (nw_find_defects) and the sampling search of
+// analysis/defects.py (nw_sample_defects, one block per sample point, at the
+// end of this file).
 //
-// Three kernels: the beads' bounding box (float min/max through order-
+// The grid search runs three kernels: the beads' bounding box (float min/max through order-
 // preserving integer atomics); every bead adds cos 2a and sin 2a of its
 // tangent angle a to its grid cell as 2^30 fixed-point integers (integer
 // atomics: the sums, and so every later result, are the same whatever the
