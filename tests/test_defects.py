@@ -102,3 +102,17 @@ def test_sampling_oracle_matches_reference(name):
 
 def test_sampling_golden_frames_keep_points():
     assert sum(len(GOLDEN[n + "_sample_kept"]) for n in SAMPLED) > 20
+
+
+@pytest.mark.parametrize("shift", [(2.0, 0.0), (-6.0, 10.0), (0.5, 0.25)])
+def test_defects_follow_a_translated_frame(shift):
+    """The grid starts at the beads' own lowest corner, so a frame moved by an
+    exact offset (in float64, as the analysis reads positions) keeps its
+    cells: the same defects, moved by the offset."""
+    pos = GOLDEN["pair_c2_pos"].astype(np.float64)
+    moved = pos + np.array(shift)
+    a = D.find_defects(pos, 5, 2.0)
+    b = D.find_defects(moved, 5, 2.0)
+    assert len(a) == len(b) > 0
+    assert np.array_equal(a["charge"], b["charge"]) and np.array_equal(a["cells"], b["cells"])
+    assert np.allclose(b["x"] - a["x"], shift[0], atol=1e-9) and np.allclose(b["y"] - a["y"], shift[1], atol=1e-9)
