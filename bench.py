@@ -14,6 +14,11 @@ both sides; the state (~190 MB) is larger than L2.  Under torchrun every rank
 runs an independent replica ("replicas only": a single system is not sharded)
 and `value` is the sum over ranks.  Reference arm: the CPU port of the
 reference's step (oracle/, FP64, all host threads) on the same workload.
+
+Other workloads (--workload): wca_dense_2m (2M beads, no solvent),
+wca_small_4k (4k beads), batch_256 (256 uneven replicas in one launch per
+step), adjoint_64x4k (differentiable 200-step rollout of 64 replicas) and
+defects_400k (the +1/2 / -1/2 defect searches on a 400k-bead frame).
 """
 from __future__ import annotations
 
