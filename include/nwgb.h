@@ -178,7 +178,9 @@ typedef enum {
 typedef enum {
     NW_POSITION = 0,      /* float4[n_total]  (beads then solvent) */
     NW_VELOCITY = 1,      /* float4[n_total] */
-    NW_TANGENT = 2,       /* float4[n_beads] */
+    NW_TANGENT = 2,       /* float4[n_beads]  (WCA worms of more than three beads on the
+                             cell-list / Verlet paths: computed from the current positions
+                             when read, the step does not store them) */
     NW_FORCE = 3,         /* float4[n_beads] */
     NW_FORCE_OLD = 4,     /* float4[n_beads] */
     NW_HASH = 5,          /* uint[n_beads]   bead cell hash of the last step (unsorted order) */
@@ -240,7 +242,10 @@ nw_status nw_get_counts(const nw_system* sys, uint32_t* n_beads, uint32_t* n_sol
 nw_status nw_set_array(nw_system* sys, int array, const void* host, uint32_t start, uint32_t count);
 /* Replaces: ParticleSystem::getArray (simulation/particleSystem.cpp:534-559). */
 nw_status nw_get_array(nw_system* sys, int array, void* host, uint32_t start, uint32_t count);
-/* Device pointer of an array (zero-copy access; valid until nw_destroy). */
+/* Device pointer of an array (zero-copy access; valid until nw_destroy).  The
+ * double-buffered state of the cell-list / Verlet paths moves between two
+ * buffers with the step parity: ask again after stepping.  NW_POSITION marks
+ * the neighbour lists for rebuilding (the caller may move beads through it). */
 nw_status nw_device_array(nw_system* sys, int array, void** dptr);
 /* Zero forces, old forces and the step counter (the reference never zeroes
  * them: simulation/particleSystem.cpp:202-203). */
