@@ -100,3 +100,30 @@ def test_reference_host_code_links_against_libnwgb(tmp_path):
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     assert exe.exists()
+
+
+def declared_arities(header: Path):
+    """{function name: number of parameters} of the header's prototypes."""
+    text = re.sub(r"/\*.*?\*/", "", header.read_text(), flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    out = {}
+    for name, params in re.findall(
+            r"^\s*(?:nw_status|void|int|uint32_t|uint64_t|size_t|const char\*)\s+(\w+)\s*\(([^;{]*?)\)\s*;",
+            text, flags=re.M | re.S):
+        p = " ".join(params.split())
+        out[name] = 0 if p in ("", "void") else p.count(",") + 1
+    return out
+
+
+@pytest.mark.parametrize("header", ["nwgb.h", "nw_legacy.h", "nwgb_batch.h", "nwgb_adjoint.h"])
+def test_python_binding_matches_every_prototype(header):
+    """Every function the ctypes binding declares has the header prototype's
+    number of parameters (a drifted signature would pass garbage)."""
+    declared = declared_arities(REPO / "include" / header)
+    bound = {name: len(args) for name, _, args in abi.HANDLE_API + abi.LEGACY_API + abi.BATCH_API + abi.ADJOINT_API}
+    checked = 0
+    for name, n in declared.items():
+        if name in bound:
+            assert bound[name] == n, (name, bound[name], n)
+            checked += 1
+    assert checked >= {"nw_legacy.h": 18, "nwgb.h": 25, "nwgb_batch.h": 12, "nwgb_adjoint.h": 6}[header], checked
