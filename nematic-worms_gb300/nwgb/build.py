@@ -23,7 +23,18 @@ BUILD_DIR = PKG_ROOT / "_build"
 ORACLE_DIR = REPO_ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "_build" / "libnworacle.so"
 REF_DIR = ORACLE_DIR / "_ref"
-REFERENCE_TREE = Path(os.environ.get("NW_REFERENCE_TREE", "/root/reference"))
+REF_CUDA_HOST = ORACLE_DIR / "_build" / "libnwref_cuda.so"
+
+
+def reference_tree() -> Path | None:
+    """The reference checkout the oracle recipes compile from: $NW_REFERENCE_TREE,
+    else a checkout named ``reference`` beside this repository; None if absent
+    (on a host without it the prebuilt oracle/_ref files are used as they are)."""
+    env = os.environ.get("NW_REFERENCE_TREE")
+    for cand in ([Path(env)] if env else []) + [REPO_ROOT.parent / "reference"]:
+        if (cand / "simulation" / "particles_kernel_impl.cuh").exists():
+            return cand
+    return None
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
@@ -109,21 +120,44 @@ def build_oracle(force: bool = False) -> Path:
 def build_reference_emulation(force: bool = False):
     """Compile the reference's own kernel source for the CPU (only where the
     reference tree exists; nothing at run time depends on it)."""
-    if not (REFERENCE_TREE / "simulation" / "particles_kernel_impl.cuh").exists():
+    tree = reference_tree()
+    if tree is None or shutil.which("make") is None:
         return None
-    args = ["make", "-s", "-C", str(ORACLE_DIR / "ref_emu"), f"REF={REFERENCE_TREE}", f"OUT={REF_DIR}",
+    args = ["make", "-s", "-C", str(ORACLE_DIR / "ref_emu"), f"REF={tree}", f"OUT={REF_DIR}",
             f"CUDA_HOME={_cuda_home()}"]
     if force:
         args.insert(1, "-B")
-    if shutil.which("make") is None:
-        return None
     _run(args)
     return REF_DIR
 
 
+def build_reference_cuda(force: bool = False):
+    """The reference CUDA build used as checker and speed denominator (test
+    infrastructure): its device code as an sm_103a fatbin, compiled from the
+    reference tree where that exists (oracle/ref_cuda/Makefile; the fatbin then
+    travels with the repository), and the host harness that loads it
+    (oracle/ref_cuda/nwref_host.cu), compiled on every host."""
+    tree = reference_tree()
+    if tree is not None and shutil.which("make") is not None:
+        args = ["make", "-s", "-C", str(ORACLE_DIR / "ref_cuda"), f"REF={tree}", f"OUT={REF_DIR}",
+                f"CUDA_HOME={_cuda_home()}"]
+        if force:
+            args.insert(1, "-B")
+        _run(args)
+    cuda = _cuda_home()
+    src = ORACLE_DIR / "ref_cuda" / "nwref_host.cu"
+    deps = [src, COMPAT / "particles_kernel.cuh"]
+    REF_CUDA_HOST.parent.mkdir(exist_ok=True)
+    if force or _newer(REF_CUDA_HOST, deps):
+        _run([str(cuda / "bin" / "nvcc")] + ARCH + ["-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC",
+              "-o", str(REF_CUDA_HOST), str(src), f"-L{cuda / 'lib64' / 'stubs'}", "-lcuda", "-lcurand"])
+    return REF_CUDA_HOST
+
+
 def build_all(force: bool = False, verbose: bool = False):
-    with ThreadPoolExecutor(max_workers=3) as ex:
+    with ThreadPoolExecutor(max_workers=4) as ex:
         f_lib = ex.submit(build_library, force, verbose)
         f_or = ex.submit(build_oracle, force)
         f_ref = ex.submit(build_reference_emulation, force)
-        return f_lib.result(), f_or.result(), f_ref.result()
+        f_rc = ex.submit(build_reference_cuda, force)
+        return f_lib.result(), f_or.result(), f_ref.result(), f_rc.result()

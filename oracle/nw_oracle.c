@@ -16,6 +16,20 @@
 #include <omp.h>
 #endif
 
+/* Per-bead force scale: when set, every force term added to bead i adds to
+ * nwo_fscale[i] (in double) the magnitude of its parts before they cancel
+ * (for a WCA pair both LJ powers, for a bond k (r + r0), for the bending
+ * projections each part, for Langevin friction and noise each).  A rounding
+ * error of relative size u in any part moves the bead's net force by at most
+ * about u times this scale, however much the parts cancel, so parity tests
+ * normalise per-bead force differences by it. */
+double* nwo_fscale = NULL;
+
+void nwo_set_force_scale(double* buf)
+{
+    nwo_fscale = buf;
+}
+
 int nwo_num_threads(void)
 {
 #ifdef _OPENMP

@@ -105,6 +105,9 @@ NWO_DECLARE(float, f32)
 NWO_DECLARE(double, f64)
 
 /* Number of host threads the oracle uses (OpenMP); 1 when built without it. */
+/* Per-bead force scale buffer (n_beads doubles, caller-zeroed) that every
+ * following force computation adds its term magnitudes to; NULL switches it off. */
+void nwo_set_force_scale(double* buf);
 int nwo_num_threads(void);
 void nwo_set_num_threads(int n);
 

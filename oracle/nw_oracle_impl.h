@@ -155,12 +155,19 @@ void RS(nwo_langevin)(const NwConfig* cfg, R* force, const R* vel, const R* nois
 {
     const R gamma = (R)cfg->gamma;
 #pragma omp parallel for schedule(static)
-    for (long long i = 0; i < (long long)n; ++i)
+    for (long long i = 0; i < (long long)n; ++i) {
         for (int a = 0; a < 3; ++a) {
             R f = (R)0 - gamma * vel[4 * i + a];
             f += noise[4 * i + a];
             force[4 * i + a] += f;
         }
+        if (nwo_fscale) {
+            const R* v = vel + 4 * i;
+            const R* z = noise + 4 * i;
+            nwo_fscale[i] += fabs((double)gamma) * sqrt((double)v[0] * v[0] + (double)v[1] * v[1] + (double)v[2] * v[2])
+                           + sqrt((double)z[0] * z[0] + (double)z[1] * z[1] + (double)z[2] * z[2]);
+        }
+    }
 }
 
 /* getTangent (simulation/particles_kernel_impl.cuh:303-309). */
@@ -176,22 +183,24 @@ static void RS(tangent)(const NwConfig* cfg, const R* a, const R* b, R* out)
 
 /* Archived harmonic bond (NWWormsKernel_InternalForce.h:37-59) of bead i to
  * bead j: dr = r_j - r_i (minimum image), F_i -= (-(k (|dr| - r0)) / |dr|) dr. */
-static void RS(wca_bond)(const NwConfig* cfg, const R* ri, const R* rj, R f[3])
+static void RS(wca_bond)(const NwConfig* cfg, const R* ri, const R* rj, R f[3], size_t i)
 {
     R dr[3] = {rj[0] - ri[0], rj[1] - ri[1], rj[2] - ri[2]};
     RS(length_periodic)(cfg, dr);
     R r = RS(rsqrt_len)(RS(dot3)(dr, dr));
     R fm = -((R)cfg->bond_k * (r - (R)cfg->bond_r0)) / r;
     for (int a = 0; a < 3; ++a) f[a] -= fm * dr[a];
+    if (nwo_fscale) nwo_fscale[i] += fabs((double)cfg->bond_k) * ((double)r + fabs((double)cfg->bond_r0));
 }
 
 /* Archived tangent drive (NWWormsKernel_DriveForce.h:21-34): F_i += F_act * unit(r_{i+1} - r_i). */
-static void RS(wca_drive)(const NwConfig* cfg, const R* ri, const R* rn, R f[3])
+static void RS(wca_drive)(const NwConfig* cfg, const R* ri, const R* rn, R f[3], size_t i)
 {
     R dr[3] = {rn[0] - ri[0], rn[1] - ri[1], rn[2] - ri[2]};
     RS(length_periodic)(cfg, dr);
     R m = RS(rsqrt_len)(RS(dot3)(dr, dr));
     for (int a = 0; a < 3; ++a) f[a] += (R)cfg->activity * (dr[a] / m);
+    if (nwo_fscale) nwo_fscale[i] += fabs((double)cfg->activity);
 }
 
 /* filamentKernel (simulation/particles_kernel_impl.cuh:751-818): bending
@@ -234,6 +243,21 @@ void RS(nwo_filament)(const NwConfig* cfg, R* force, R* tangent, const R* pos, u
                 force[4 * (i + 1) + a] += fj[a];
                 force[4 * (i + 2) + a] += fk[a];
             }
+            if (nwo_fscale) {
+                /* per component A (|r_jk| + |r_ij| |r_jk| / |r_ij|) for F_i and
+                 * A (|r_ij| + |r_jk| |r_ij| / |r_jk|) for F_k: the magnitudes
+                 * of the projections before they cancel */
+                double Ad = fabs((double)A), si = 0, sk = 0;
+                for (int a = 0; a < 3; ++a) {
+                    double ui = Ad * (fabs((double)rjk[a]) + fabs((double)rij[a]) * (double)djk / (double)dij);
+                    double uk = Ad * (fabs((double)rij[a]) + fabs((double)rjk[a]) * (double)dij / (double)djk);
+                    si += ui * ui;
+                    sk += uk * uk;
+                }
+                nwo_fscale[i] += sqrt(si);
+                nwo_fscale[i + 2] += sqrt(sk);
+                nwo_fscale[i + 1] += sqrt(si) + sqrt(sk);
+            }
             force[4 * i + 3] += 0;
             RS(tangent)(cfg, ri, rk, tangent + 4 * (i + 1));
             if (p == 0) RS(tangent)(cfg, ri, rj, tangent + 4 * i);
@@ -243,9 +267,9 @@ void RS(nwo_filament)(const NwConfig* cfg, R* force, R* tangent, const R* pos, u
             for (uint32_t c = 0; c < L; ++c) {
                 size_t i = head + c;
                 R f[3] = {force[4 * i], force[4 * i + 1], force[4 * i + 2]};
-                if (c + 1 < L) RS(wca_bond)(cfg, pos + 4 * i, pos + 4 * (i + 1), f);
-                if (c > 0) RS(wca_bond)(cfg, pos + 4 * i, pos + 4 * (i - 1), f);
-                if (c + 1 < L) RS(wca_drive)(cfg, pos + 4 * i, pos + 4 * (i + 1), f);
+                if (c + 1 < L) RS(wca_bond)(cfg, pos + 4 * i, pos + 4 * (i + 1), f, i);
+                if (c > 0) RS(wca_bond)(cfg, pos + 4 * i, pos + 4 * (i - 1), f, i);
+                if (c + 1 < L) RS(wca_drive)(cfg, pos + 4 * i, pos + 4 * (i + 1), f, i);
                 for (int a = 0; a < 3; ++a) force[4 * i + a] = f[a];
             }
         }
@@ -294,6 +318,32 @@ static void RS(ref_extensile)(const NwConfig* cfg, const R* ra, const R* rb, con
         R den = (R)2 * d;
         for (int a = 0; a < 3; ++a) out[a] = (-(R)cfg->activity * (ta[a] - tb[a])) / den;
     }
+}
+
+/* Force scale of one REF_DEM neighbour (bond or contact, plus the
+ * extensile term between filaments): the term magnitudes before their
+ * differences cancel. */
+static double RS(ref_term_scale)(const NwConfig* cfg, const R* ra, const R* rb, const R* va, const R* vb, const R* ta,
+                                 const R* tb, int same, int bonded)
+{
+    R rel[3] = {rb[0] - ra[0], rb[1] - ra[1], rb[2] - ra[2]};
+    double d = (double)RS(length_periodic)(cfg, rel), out = 0;
+    if (bonded) {
+        out = fabs((double)cfg->bond_k) * (fabs((double)cfg->bond_r0) + d);
+    } else {
+        double cd = 2.0 * (double)cfg->radius;
+        if (d < cd) {
+            double sv = sqrt((double)va[0] * va[0] + (double)va[1] * va[1] + (double)va[2] * va[2])
+                      + sqrt((double)vb[0] * vb[0] + (double)vb[1] * vb[1] + (double)vb[2] * vb[2]);
+            out = fabs((double)cfg->spring) * (cd + d) + fabs((double)cfg->damping) * sv + 2.0 * fabs((double)cfg->shear) * sv;
+        }
+    }
+    if (!same && RS(dot3)(ta, tb) < (R)-0.5) {
+        double st = sqrt((double)ta[0] * ta[0] + (double)ta[1] * ta[1] + (double)ta[2] * ta[2])
+                  + sqrt((double)tb[0] * tb[0] + (double)tb[1] * tb[1] + (double)tb[2] * tb[2]);
+        out += fabs((double)cfg->activity) * st / (2.0 * d);
+    }
+    return out;
 }
 
 /* Grid coordinate of a position (calcGridPos, :231-238), FP32 arithmetic. */
@@ -353,6 +403,9 @@ static void RS(pair_ref)(const NwConfig* cfg, R* force, const R* sp, const R* sv
                             if (same && ((cI + 1u == cJ) || (cI - 1u == cJ))) RS(ref_bond)(cfg, r, r2, f);
                             else RS(ref_collide)(cfg, r, r2, v, v2, f);
                             for (int a = 0; a < 3; ++a) cs[a] += f[a];
+                            if (nwo_fscale)
+                                nwo_fscale[sorted_index[p]] +=
+                                    RS(ref_term_scale)(cfg, r, r2, v, v2, t, t2, same, same && ((cI + 1u == cJ) || (cI - 1u == cJ)));
                             if (!same) {
                                 RS(ref_extensile)(cfg, r, r2, t, t2, f);
                                 for (int a = 0; a < 3; ++a) cs[a] += f[a];
@@ -454,6 +507,11 @@ static void RS(pair_wca)(const NwConfig* cfg, R* force, const R* sp, const uint3
                         if (rr > rc2) continue;
                         R fm = RS(lj_mag)(cfg, rr);
                         for (int a = 0; a < 3; ++a) f[a] -= fm * dr[a];
+                        if (nwo_fscale) {
+                            double rrd = (double)rr, s6 = pow((double)cfg->lj_sigma, 6.0);
+                            double amp = fabs(24.0 * (double)cfg->lj_epsilon * s6);
+                            nwo_fscale[me] += amp * (2.0 * s6 / pow(rrd, 7.0) + 1.0 / (rrd * rrd * rrd * rrd)) * sqrt(rrd);
+                        }
                     }
                 }
         for (int a = 0; a < 3; ++a) force[4 * (size_t)me + a] += f[a];

@@ -53,6 +53,7 @@ def lib() -> C.CDLL:
         L.nwo_num_cells.argtypes = [_CP]
         L.nwo_num_srd_cells.restype = _u32
         L.nwo_num_srd_cells.argtypes = [_CP]
+        L.nwo_set_force_scale.argtypes = [_P]
         L.nwo_num_threads.restype = C.c_int
         L.nwo_set_num_threads.argtypes = [C.c_int]
         for s, R in (("f32", C.c_float), ("f64", C.c_double)):
@@ -154,6 +155,23 @@ def bead_sort(cfg: NwConfig, pos):
 
 # ---- physics ---------------------------------------------------------------------
 
+class force_scale:
+    """Collects the per-bead force scale (sum of force-term magnitudes before
+    cancellation, float64) of the oracle calls made inside the block:
+    ``with force_scale(n) as S: pair(...)`` leaves it in S.values."""
+
+    def __init__(self, n: int):
+        self.values = np.zeros(max(int(n), 1), np.float64)
+
+    def __enter__(self):
+        lib().nwo_set_force_scale(_ptr(self.values))
+        return self
+
+    def __exit__(self, *exc):
+        lib().nwo_set_force_scale(None)
+        return False
+
+
 def integrate(cfg, pos, vel, force, force_old, dt, prec=32):
     dt_, s = _dt(prec)
     p, v, f, fo = (_f4(a, dt_) for a in (pos, vel, force, force_old))
@@ -238,8 +256,11 @@ def srd_shift(cfg, step, prec=32):
     return np.array(list(o), dtype=np.float32)
 
 
-def step(cfg, state, step_index, dt, prec=32):
-    """One full step; state = dict(pos, vel, force, force_old, tangent)."""
+def step(cfg, state, step_index, dt, prec=32, force_scale=False):
+    """One full step; state = dict(pos, vel, force, force_old, tangent).
+    With force_scale, the result also holds ``force_scale``: per bead the sum
+    of the magnitudes of every force term of the step (float64), the scale
+    that bounds the rounding error of the bead's net force."""
     dt_, s = _dt(prec)
     p, v, f, fo, t = (_f4(state[k], dt_) for k in ("pos", "vel", "force", "force_old", "tangent"))
     nb = cfg.n_beads
@@ -248,9 +269,17 @@ def step(cfg, state, step_index, dt, prec=32):
     si = np.empty(nb, np.uint32)
     cs = np.empty(nc, np.uint32)
     ce = np.empty(nc, np.uint32)
-    getattr(lib(), f"nwo_step_{s}")(C.byref(cfg), _ptr(p), _ptr(v), _ptr(f), _ptr(fo), _ptr(t), step_index, dt,
-                                    _ptr(h), _ptr(si), _ptr(cs), _ptr(ce))
-    return dict(pos=p, vel=v, force=f, force_old=fo, tangent=t, hash=h, sorted_index=si, cell_start=cs, cell_end=ce)
+    fs = np.zeros(max(nb, 1), np.float64) if force_scale else None
+    lib().nwo_set_force_scale(_ptr(fs))
+    try:
+        getattr(lib(), f"nwo_step_{s}")(C.byref(cfg), _ptr(p), _ptr(v), _ptr(f), _ptr(fo), _ptr(t), step_index, dt,
+                                        _ptr(h), _ptr(si), _ptr(cs), _ptr(ce))
+    finally:
+        lib().nwo_set_force_scale(None)
+    out = dict(pos=p, vel=v, force=f, force_old=fo, tangent=t, hash=h, sorted_index=si, cell_start=cs, cell_end=ce)
+    if force_scale:
+        out["force_scale"] = fs[:nb]
+    return out
 
 
 def set_threads(n: int) -> None:

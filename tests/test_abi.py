@@ -14,7 +14,13 @@ import pytest
 from conftest import REPO
 from nwgb import abi
 
-REFERENCE = Path("/root/reference")
+def _reference():
+    from nwgb.build import reference_tree
+
+    return reference_tree() or Path("/nonexistent")
+
+
+REFERENCE = _reference()
 
 
 def declared_functions(header: Path):

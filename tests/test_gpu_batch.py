@@ -1,15 +1,15 @@
-"""Batched replicas against single systems: each replica of a batch follows
-the same trajectory as a single-system handle with its configuration (same
-strategy, same launch-independent arithmetic) up to the order of FP32 sums,
-and the batch reports its launches, tuning and errors."""
+"""Batched replicas: every replica of a batch against the oracle's step of
+its own configuration, per bead (tests/parity.py); against a single-system
+handle of the same configuration over a trajectory (same strategy, up to the
+order of FP32 sums); launches, tuning and errors."""
 from __future__ import annotations
 
 import numpy as np
 import pytest
 
-from conftest import rel_err
 from nwgb import abi
 from nwgb.init import batch_configs, initial_state
+from parity import TOL, force_err, fp64_bound, update_err, vec_err
 
 pytestmark = pytest.mark.gpu
 
@@ -32,9 +32,53 @@ def run_single(cfg, pos, vel, nsteps, strategy):
         return s.get_array(abi.NW_POSITION), s.get_array(abi.NW_VELOCITY), s.get_array(abi.NW_FORCE)
 
 
+def periodic_box(cfg):
+    return np.array([cfg.box[a] if cfg.boundary[a] == abi.NW_PERIODIC else 0.0 for a in range(3)])
+
+
+@pytest.mark.parametrize("strategy", [abi.NW_STRATEGY_VERLET, abi.NW_STRATEGY_CELL_LISTS])
+def test_batch_replicas_match_oracle(lib, orc, strategy):
+    """One step of every replica of an uneven batch (worm counts, lengths,
+    F_act, k_bend, boxes differ) from a state with non-zero forces, against
+    the FP32 and FP64 oracle steps of that replica's configuration: forces
+    per bead within 1e-5 of the force scale, velocities relative, positions
+    relative to the displacement."""
+    import nwgb
+
+    cfgs, states = small_batch(lib, n=7, seed=13)
+    starts = []
+    for r, (c, (pos, vel)) in enumerate(zip(cfgs, states)):
+        z = np.zeros((c.n_beads, 4), np.float32)
+        s1 = orc.step(c, dict(pos=pos, vel=vel, force=z, force_old=z, tangent=z), 0, c.dt, 32)
+        starts.append(s1)
+    with nwgb.Batch(cfgs) as b:
+        b.set_tuning(256, strategy, 0.3)
+        for r, s1 in enumerate(starts):
+            b.set_array(r, abi.NW_POSITION, s1["pos"])
+            b.set_array(r, abi.NW_VELOCITY, s1["vel"])
+            b.set_array(r, abi.NW_FORCE, s1["force"])
+            b.set_array(r, abi.NW_FORCE_OLD, s1["force_old"])
+        b.step(1)
+        b.sync()
+        got = [{k: b.get_array(r, a) for k, a in (("pos", abi.NW_POSITION), ("vel", abi.NW_VELOCITY),
+                                                   ("force", abi.NW_FORCE), ("force_old", abi.NW_FORCE_OLD))}
+               for r in range(len(cfgs))]
+    for r, (c, s1, g) in enumerate(zip(cfgs, starts, got)):
+        st = {k: s1[k] for k in ("pos", "vel", "force", "force_old", "tangent")}
+        o = orc.step(c, st, 0, c.dt, 32)
+        o64 = orc.step(c, st, 0, c.dt, 64, force_scale=True)
+        assert np.array_equal(g["force_old"][:, :3], s1["force"][:, :3]), r
+        S, box = o64["force_scale"], periodic_box(c)
+        for m in (lambda x, y: force_err(x["force"], y["force"], S),
+                  lambda x, y: vec_err(x["vel"], y["vel"]),
+                  lambda x, y: update_err(x["pos"], y["pos"], s1["pos"], box)):
+            assert m(g, o) < TOL, r
+            assert m(g, o64) < fp64_bound(m(o, o64)), r
+
+
 @pytest.mark.parametrize("strategy", [abi.NW_STRATEGY_VERLET, abi.NW_STRATEGY_CELL_LISTS])
 @pytest.mark.parametrize("threads", [128, 256, 512])
-def test_batch_matches_single_systems(lib, strategy, threads):
+def test_batch_matches_single_systems(lib, orc, strategy, threads):
     import nwgb
 
     cfgs, states = small_batch(lib)
@@ -52,9 +96,15 @@ def test_batch_matches_single_systems(lib, strategy, threads):
         for r, c in enumerate(cfgs):
             c.neighbor_skin = 0.3
             p, v, f = run_single(c, *states[r], n, strategy)
-            assert rel_err(b.get_array(r, abi.NW_POSITION), p) < 1e-5, r
-            assert rel_err(b.get_array(r, abi.NW_VELOCITY), v) < 1e-4, r
-            assert rel_err(b.get_array(r, abi.NW_FORCE), f) < 1e-3, r
+            # 25 steps apart from any common state: per-bead differences are
+            # FP32 summation-order differences grown along the trajectory
+            z = np.zeros((c.n_beads, 4), np.float32)
+            st = dict(pos=states[r][0], vel=states[r][1], force=z, force_old=z, tangent=z)
+            for k in range(n):
+                st = orc.step(c, st, k, c.dt, 64, force_scale=k == n - 1)
+            assert update_err(b.get_array(r, abi.NW_POSITION), p, states[r][0], periodic_box(c)) < 1e-4, r
+            assert vec_err(b.get_array(r, abi.NW_VELOCITY), v) < 1e-4, r
+            assert force_err(b.get_array(r, abi.NW_FORCE), f, st["force_scale"]) < 1e-4, r
 
 
 def test_batch_graph_replay_is_deterministic(lib):

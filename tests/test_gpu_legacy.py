@@ -3,7 +3,9 @@ golden vectors of the reference's own kernels (tests/golden) and the oracle.
 
 Device buffers come from torch (memory plumbing only); every call goes
 through the library's extern "C" entry points.  Tolerance: bit-exact for
-hashes, sort order and cell bounds; 1e-5 of max |reference| for floats.
+hashes, sort order and cell bounds; per bead 1e-5 for floats (tests/parity.py:
+forces against the FP64 oracle's force scale of the same call, velocities and
+tangents relative, positions relative to the bead's displacement).
 """
 from __future__ import annotations
 
@@ -12,8 +14,9 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, rel_err
+from conftest import GOLDEN
 from nwgb.abi import NwConfig
+from parity import force_err, update_err, vec_err
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-5
@@ -48,28 +51,43 @@ def set_legacy_params(lib, cfg: NwConfig, shift=(0.0, 0.0, 0.0)):
     return set_parameters(lib, cfg, shift)
 
 
+def norms(a):
+    return np.linalg.norm(np.asarray(a, np.float64)[:, :3], axis=1)
+
+
+def box_of(cfg):
+    return np.array([cfg.box[a] if cfg.boundary[a] == 0 else 0.0 for a in range(3)])
+
+
 @pytest.mark.parametrize("name", ["ref_dem_2d.npz", "ref_dem_3d_walls.npz"])
-def test_legacy_bead_pipeline_matches_reference(lib, name):
+def test_legacy_bead_pipeline_matches_reference(lib, orc, name):
     cfg, d = load(name)
     set_legacy_params(lib, cfg)
     nb = cfg.n_beads
     p, v = torch_dev(d["pos_in"]), torch_dev(d["vel_in"])
     f, fo = torch_dev(d["force_in"]), torch_dev(d["force_old_in"])
     lib.integrateFilaments(ptr(p), ptr(v), ptr(f), ptr(fo), float(d["dt"]), nb)
-    assert rel_err(host(p), d["int_pos"]) < TOL and rel_err(host(v), d["int_vel"]) < TOL
+    assert update_err(host(p), d["int_pos"], d["pos_in"], box_of(cfg)) < TOL
+    assert vec_err(host(v), d["int_vel"]) < TOL
     assert np.array_equal(host(f), d["int_force"]) and np.array_equal(host(fo), d["int_force_old"])
     # Langevin kernel with the injected noise
     noise = torch_dev(d["noise"])
     p, v = torch_dev(d["int_pos"]), torch_dev(d["int_vel"])
     f = torch_dev(d["int_force"])
     lib.nw_legacy_langevin_apply(ptr(f), ptr(v), ptr(noise), nb)
-    assert rel_err(host(f), d["lang_force"]) < TOL
+    with orc.force_scale(nb) as S:
+        orc.langevin(cfg, d["int_force"], d["int_vel"], d["noise"], prec=64)
+    S_lang = norms(d["int_force"]) + S.values[:nb]
+    assert force_err(host(f), d["lang_force"], S_lang) < TOL
     # bending + tangents
     f = torch_dev(d["lang_force"])
     t = torch_dev(d["tan_in"])
     lib.filamentForces(ptr(f), ptr(t), ptr(p), float(cfg.num_filaments))
-    assert rel_err(host(f), d["fil_force"]) < TOL
-    assert rel_err(host(t), d["fil_tan"]) < TOL
+    with orc.force_scale(nb) as S:
+        orc.filament(cfg, d["lang_force"], d["tan_in"], d["int_pos"], prec=64)
+    S_fil = S_lang + S.values[:nb]
+    assert force_err(host(f), d["fil_force"], S_fil) < TOL
+    assert vec_err(host(t), d["fil_tan"]) < TOL
     # hash -> sort -> reorder: bit-exact
     import torch
 
@@ -101,7 +119,10 @@ def test_legacy_bead_pipeline_matches_reference(lib, name):
     lib.collideFilaments(ptr(f), *[ptr(b) for b in bufs], nb, ncell)
     torch.cuda.synchronize()
     del bufs
-    assert rel_err(host(f), d["collide_force"]) < TOL
+    with orc.force_scale(nb) as S:
+        orc.pair(cfg, d["fil_force"], d["int_pos"], d["int_vel"], d["fil_tan"], d["sorted_index"], d["cell_start"],
+                 d["cell_end"], prec=64)
+    assert force_err(host(f), d["collide_force"], S_fil + S.values[:nb]) < TOL
     assert lib.nw_legacy_last_status() == 0
 
 
@@ -140,15 +161,19 @@ def test_legacy_srd_pipeline_matches_reference(lib):
     csn = host(cs).view(np.uint32)[:nsc]
     assert np.array_equal(csn, d["cell_start"])
     lib.solventIsokineticThermostat(ptr(v), ptr(sv), ptr(cs), ptr(ce), ptr(ix), nsc)
-    assert rel_err(host(v), d["thermo_vel"]) < TOL
+    assert vec_err(host(v), d["thermo_vel"]) < TOL
     com = torch.zeros((nsc, 4), dtype=torch.float32, device="cuda")
     lib.solventCellCentorOfMomentum(ptr(com), ptr(sv), ptr(cs), ptr(ce), ptr(ix), nsc)
-    assert rel_err(host(com), d["com"]) < TOL
+    assert vec_err(host(com), d["com"]) < TOL
     uni = torch_dev(d["uniform"])
     lib.nw_legacy_collide_solvent_apply(ptr(p), ptr(v), ptr(com), ptr(uni), n)
-    assert rel_err(host(v), d["coll_vel"]) < TOL
+    assert vec_err(host(v), d["coll_vel"]) < TOL
+    p_before = host(p)
     lib.integrateSolvent(ptr(p), ptr(v), float(d["dt_srd"]), cfg.n_beads, cfg.n_solvent)
-    assert rel_err(host(p), d["pos_out"]) < TOL and rel_err(host(v), d["vel_out"]) < TOL
+    nb = cfg.n_beads
+    assert np.array_equal(host(p)[:nb], d["pos_out"][:nb])
+    assert update_err(host(p)[nb:], d["pos_out"][nb:], p_before[nb:], box_of(cfg)) < TOL
+    assert vec_err(host(v), d["vel_out"]) < TOL
 
 
 def test_legacy_sort_is_stable_for_arbitrary_keys(lib):

@@ -1,12 +1,11 @@
 """Parity of the CUDA step (through the C ABI) with the CPU oracle.
 
-Tolerances: cell hashes, sort order and cell bounds bit-exact; positions,
-velocities and forces within 1e-5 of the FP32 oracle, measured as
-max |gpu - oracle| / max |oracle| per array.  The FP64 oracle's error is
-reported alongside and bounded at 1e-3: FP32 itself is that far from FP64 on
-the net force of beads in WCA contact (pair terms ~r^-14 that cancel; the
-FP32 oracle shows the same 1.6e-4 on the SRD case, where no Langevin noise
-sets the force scale).
+Tolerances (tests/parity.py): cell hashes, sort order and cell bounds
+bit-exact; per bead, forces within 1e-5 of the bead's force scale, velocities
+and tangents within 1e-5 relative, the one-step position update within 1e-5
+of the bead's displacement (up to the final FP32 rounding), against the FP32
+oracle; against the FP64 oracle within 1e-5 or the FP32 oracle's own FP64
+error, whichever is larger.
 """
 from __future__ import annotations
 
@@ -15,14 +14,11 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from conftest import rel_err
 from nwgb import abi
 from nwgb.init import initial_state, reference_reset, wca_config
+from parity import SOLVENT_FLOOR, TOL, force_err, fp64_bound, summary, update_err, vec_err
 
 pytestmark = pytest.mark.gpu
-
-TOL32 = 1e-5
-TOL64 = 1e-3
 
 
 def make_case(kind: str, lib):
@@ -126,7 +122,7 @@ def lattice_3d(cfg, seed):
     return pos, vel, np.zeros_like(pos)
 
 
-def run_gpu(cfg, pos, vel, tan, nsteps=1, graphs=True):
+def run_gpu(cfg, pos, vel, tan, nsteps=1, graphs=True, force=None, force_old=None, step=0):
     import nwgb
 
     s = nwgb.System(cfg)
@@ -134,6 +130,11 @@ def run_gpu(cfg, pos, vel, tan, nsteps=1, graphs=True):
     s.set_array(abi.NW_POSITION, pos)
     s.set_array(abi.NW_VELOCITY, vel)
     s.set_array(abi.NW_TANGENT, tan)
+    if force is not None:
+        s.set_array(abi.NW_FORCE, force)
+        s.set_array(abi.NW_FORCE_OLD, force_old)
+    if step:
+        s.set_step(step)
     s.step(nsteps, cfg.dt)
     s.sync()
     out = {k: s.get_array(a) for k, a in (("pos", abi.NW_POSITION), ("vel", abi.NW_VELOCITY),
@@ -146,12 +147,44 @@ def run_gpu(cfg, pos, vel, tan, nsteps=1, graphs=True):
     return out
 
 
-def run_oracle(orc, cfg, pos, vel, tan, nsteps=1, prec=32):
+def run_oracle(orc, cfg, pos, vel, tan, nsteps=1, prec=32, force=None, force_old=None, step=0, force_scale=False):
     z = np.zeros((cfg.n_beads, 4), np.float32)
-    st = dict(pos=pos, vel=vel, force=z, force_old=z, tangent=tan)
+    st = dict(pos=pos, vel=vel, force=z if force is None else force, force_old=z if force_old is None else force_old,
+              tangent=tan)
     for k in range(nsteps):
-        st = orc.step(cfg, st, k, cfg.dt, prec)
+        st = orc.step(cfg, st, step + k, cfg.dt, prec, force_scale=force_scale and k == nsteps - 1)
     return st
+
+
+def periodic_box(cfg):
+    """Box lengths of the periodic axes (0 for walls): the minimum image of a displacement."""
+    return np.array([cfg.box[a] if cfg.boundary[a] == abi.NW_PERIODIC else 0.0 for a in range(3)])
+
+
+def check_step_parity(cfg, g, o, o64, pos0):
+    """Bit-exact integer outputs; per-bead float parity against the FP32 and
+    the FP64 oracle (module docstring)."""
+    nb = cfg.n_beads
+    assert np.array_equal(g["hash"], o["hash"])
+    assert np.array_equal(g["sorted_index"], o["sorted_index"])
+    assert np.array_equal(g["cell_start"], o["cell_start"])
+    ne = o["cell_start"] != abi.EMPTY
+    assert np.array_equal(g["cell_end"][ne], o["cell_end"][ne])
+    # the old force is the previous step's force, copied by the integrator
+    assert np.array_equal(g["force_old"][:, :3], o["force_old"][:, :3])
+    S = o64["force_scale"]
+    box = periodic_box(cfg)
+    metrics = {
+        "force": lambda x, y: force_err(x["force"], y["force"], S),
+        "vel": lambda x, y: vec_err(x["vel"][:nb], y["vel"][:nb]),
+        "tangent": lambda x, y: vec_err(x["tangent"], y["tangent"]),
+        "displacement": lambda x, y: update_err(x["pos"][:nb], y["pos"][:nb], pos0[:nb], box),
+    }
+    for k, m in metrics.items():
+        e32 = m(g, o)
+        assert e32 < TOL, (k, "fp32", e32, summary(g[k if k != "displacement" else "pos"], o[k if k != "displacement" else "pos"]))
+        e64 = m(g, o64)
+        assert e64 < fp64_bound(m(o, o64)), (k, "fp64", e64, m(o, o64))
 
 
 CASES = ["wca", "wca_srd", "wca_srd_dense", "wca_srd_rounds", "wca_srd_packed", "wca_reverse", "wca_3d", "ref", "ref_srd", "ref_walls", "ref_3d"]
@@ -169,32 +202,60 @@ def strategy_applies(kind, strategy):
 @pytest.mark.parametrize("strategy", STRATEGIES)
 @pytest.mark.parametrize("kind", CASES)
 def test_one_step_matches_oracle(lib, orc, kind, strategy):
+    """Step 0 from rest forces (f = f_old = 0): hashes, sort and cell bounds,
+    the forces of the step, tangents, and the SRD collision of step 0."""
     if not strategy_applies(kind, strategy):
         pytest.skip("Verlet lists are WCA-only")
     cfg, pos, vel, tan = make_case(kind, lib)
     cfg.strategy = strategy
     g = run_gpu(cfg, pos, vel, tan)
     o = run_oracle(orc, cfg, pos, vel, tan, 1, 32)
-    o64 = run_oracle(orc, cfg, pos, vel, tan, 1, 64)
+    o64 = run_oracle(orc, cfg, pos, vel, tan, 1, 64, force_scale=True)
+    check_step_parity(cfg, g, o, o64, pos)
     nb = cfg.n_beads
-    assert np.array_equal(g["hash"], o["hash"])
-    assert np.array_equal(g["sorted_index"], o["sorted_index"])
-    assert np.array_equal(g["cell_start"], o["cell_start"])
-    ne = o["cell_start"] != abi.EMPTY
-    assert np.array_equal(g["cell_end"][ne], o["cell_end"][ne])
-    for k in ("pos", "vel", "force", "force_old", "tangent"):
-        a = g[k][:nb] if k in ("pos", "vel") else g[k]
-        b = o[k][:nb] if k in ("pos", "vel") else o[k]
-        assert rel_err(a, b) < TOL32, (k, rel_err(a, b))
-        b64 = o64[k][:nb] if k in ("pos", "vel") else o64[k]
-        assert rel_err(a, b64) < TOL64, (k, "fp64", rel_err(a, b64))
     bead, srd = LAUNCHES[strategy]
-    if cfg.srd_enabled:  # solvent after the collision of step 0
-        assert rel_err(g["pos"][nb:], o["pos"][nb:]) < TOL32
-        assert rel_err(g["vel"][nb:], o["vel"][nb:]) < TOL32
+    if cfg.srd_enabled:  # solvent after the collision of step 0, particle by particle
+        box = periodic_box(cfg)
+        before = ref_streamed_from(o, cfg)
+        sv = lambda x, y: vec_err(x["vel"][nb:], y["vel"][nb:], SOLVENT_FLOOR)  # noqa: E731
+        sp = lambda x, y: update_err(x["pos"][nb:], y["pos"][nb:], before, box, SOLVENT_FLOOR)  # noqa: E731
+        for m in (sv, sp):
+            assert m(g, o) < TOL, m(g, o)
+            assert m(g, o64) < fp64_bound(m(o, o64)), (m(g, o64), m(o, o64))
         assert g["launches"] == bead + srd + 1
     else:
         assert g["launches"] == bead + 1
+
+
+def ref_streamed_from(ref, cfg):
+    """Solvent positions before the streaming of the collision that ends the
+    step: the streamed position minus velocity x srd_gap x dt."""
+    nb = cfg.n_beads
+    p = np.asarray(ref["pos"][nb:], np.float64)[:, :3]
+    v = np.asarray(ref["vel"][nb:], np.float64)[:, :3]
+    return p - v * (cfg.srd_gap * cfg.dt)
+
+
+@pytest.mark.parametrize("strategy", STRATEGIES)
+@pytest.mark.parametrize("kind", [c for c in CASES if "srd" not in c or c == "wca_srd"] + ["ref_srd"])
+def test_update_from_forced_state_matches_oracle(lib, orc, kind, strategy):
+    """Step 1 from the oracle's state after step 0 (non-zero f and f_old): the
+    velocity-Verlet update v += (f + f_old) dt / 2, r += v dt + f dt^2 / 2 of
+    every bead, then the next forces, per bead against FP32 and FP64."""
+    if not strategy_applies(kind, strategy):
+        pytest.skip("Verlet lists are WCA-only")
+    cfg, pos, vel, tan = make_case(kind, lib)
+    cfg.strategy = strategy
+    s1 = run_oracle(orc, cfg, pos, vel, tan, 1, 32)
+    nb = cfg.n_beads
+    assert np.abs(s1["force"][:, :3]).max() > 0 and np.abs(s1["force_old"]).max() == 0
+    st = dict(pos=s1["pos"], vel=s1["vel"], tan=s1["tangent"], force=s1["force"], force_old=s1["force_old"])
+    g = run_gpu(cfg, st["pos"], st["vel"], st["tan"], force=st["force"], force_old=st["force_old"], step=1)
+    o = run_oracle(orc, cfg, st["pos"], st["vel"], st["tan"], 1, 32, force=st["force"], force_old=st["force_old"],
+                   step=1)
+    o64 = run_oracle(orc, cfg, st["pos"], st["vel"], st["tan"], 1, 64, force=st["force"],
+                     force_old=st["force_old"], step=1, force_scale=True)
+    check_step_parity(cfg, g, o, o64, st["pos"])
 
 
 @pytest.mark.parametrize("strategy", STRATEGIES)
@@ -213,7 +274,7 @@ def test_graph_replay_is_bit_identical_to_direct_launches(lib, kind, strategy):
 
 
 @pytest.mark.parametrize("kind", ["wca", "wca_srd", "ref"])
-def test_strategies_agree(lib, kind):
+def test_strategies_agree(lib, orc, kind):
     """Cell lists visit each cell's beads in index order, as the sorted
     arrays do: both strategies give the same cell assignment and sort order
     and the same trajectory up to FP32 contraction differences of the two
@@ -224,11 +285,19 @@ def test_strategies_agree(lib, kind):
         if strategy_applies(kind, strategy):
             cfg.strategy = strategy
             out.append(run_gpu(cfg, pos, vel, tan, nsteps=15, graphs=True))
+    nb = cfg.n_beads
+    S = run_oracle(orc, cfg, pos, vel, tan, 15, 64, force_scale=True)["force_scale"]
+    box = periodic_box(cfg)
     for o in out[1:]:
         for k in ("hash", "sorted_index", "cell_start"):
             assert np.array_equal(out[0][k], o[k]), k
-        for k in ("pos", "vel", "force", "force_old", "tangent"):
-            assert rel_err(out[0][k], o[k]) < 1e-5, k
+        # 15 steps of the same dynamics; the strategies sum pair forces in
+        # different orders, and those FP32 differences grow along the trajectory
+        assert update_err(o["pos"][:nb], out[0]["pos"][:nb], pos[:nb], box) < 1e-4
+        assert vec_err(o["vel"][:nb], out[0]["vel"][:nb]) < 1e-4
+        assert vec_err(o["tangent"], out[0]["tangent"]) < 1e-4
+        for k in ("force", "force_old"):
+            assert force_err(o[k], out[0][k], S) < 1e-4, k
 
 
 @pytest.mark.parametrize("skin", [0.02, 0.3, 1.0])
@@ -244,9 +313,12 @@ def test_verlet_lists_track_oracle_across_rebuilds(lib, orc, skin):
     g = run_gpu(cfg, pos, vel, tan, nsteps=n)
     cfg.strategy = abi.NW_STRATEGY_SORTED
     s = run_gpu(cfg, pos, vel, tan, nsteps=n)
-    # same dynamics as the reference-order path up to FP32 summation order
-    assert rel_err(g["pos"], s["pos"]) < 1e-5
-    assert rel_err(g["force"], s["force"]) < 1e-3
+    # same dynamics as the reference-order path up to FP32 summation order,
+    # amplified over 40 steps of a hot (kT = 2) system
+    box = periodic_box(cfg)
+    S = run_oracle(orc, cfg, pos, vel, tan, n, 64, force_scale=True)["force_scale"]
+    assert update_err(g["pos"], s["pos"], pos, box) < 1e-4
+    assert force_err(g["force"], s["force"], S) < 1e-4
     # the reference-grid hash of the Verlet system is computed when read
     assert np.mean(g["hash"] == s["hash"]) > 0.999
 
@@ -275,8 +347,11 @@ def test_short_trajectory_tracks_oracle(lib, orc, kind):
     o = run_oracle(orc, cfg, pos, vel, tan, n, 32)
     nb = cfg.n_beads
     # trajectories separate only by accumulated FP32 rounding over 12 steps
-    assert rel_err(g["pos"][:nb], o["pos"][:nb]) < 1e-5
-    assert rel_err(g["force"], o["force"]) < 1e-3
+    o64 = run_oracle(orc, cfg, pos, vel, tan, n, 64, force_scale=True)
+    box = periodic_box(cfg)
+    assert update_err(g["pos"][:nb], o["pos"][:nb], pos[:nb], box) < 1e-4
+    assert vec_err(g["vel"][:nb], o["vel"][:nb]) < 1e-4
+    assert force_err(g["force"], o["force"], o64["force_scale"]) < 1e-4
     assert np.mean(g["sorted_index"] == o["sorted_index"]) > 0.999
 
 

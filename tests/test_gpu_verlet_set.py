@@ -8,7 +8,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import rel_err
+from parity import update_err
 from nwgb import abi
 from nwgb.init import initial_state, wca_config
 
@@ -70,7 +70,9 @@ def test_small_move_keeps_lists_and_tracks_a_rebuilt_system(lib):
         b.sync()
         pa, _ = state(a)
         pb, _ = state(b)
-    assert rel_err(pa[:nb], pb[:nb]) < 1e-5
+    # the same trajectory up to FP32 summation order: per bead, the positions
+    # agree to 1e-5 of the displacement since they were set
+    assert update_err(pa[:nb], pb[:nb], p, None) < 1e-5
 
 
 def test_large_move_rebuilds_the_lists(lib):
