@@ -8,12 +8,21 @@ one ParticleSystem::update equivalent (the SRD sub-step every 10th step).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Our arm: K steps replayed from CUDA graphs of 10 steps (one SRD period), timed
-with CUDA events on the engine's stream between a barrier + synchronize on
-both sides; the state (~190 MB) is larger than L2.  Under torchrun every rank
-runs an independent replica ("replicas only": a single system is not sharded)
-and `value` is the sum over ranks.  Reference arm: the CPU port of the
-reference's step (oracle/, FP64, all host threads) on the same workload.
+Our arm: exactly W warm-up steps, then K steps replayed from CUDA graphs of 10
+steps (one SRD period; every graph the timed region replays is captured
+beforehand), timed with CUDA events on the engine's stream between a barrier +
+synchronize on both sides; the timed region is repeated three times from the
+same checkpoint and `value` is the median (`timing` gives all three).  The
+state (~190 MB) is larger than L2.  Under torchrun every rank runs an
+independent replica ("replicas only": a single system is not sharded) and
+`value` is the sum over ranks.  Sub-blocks of the same line: `strategies`
+(the same workload under the sorted-scheme, cell-list and Verlet strategies),
+`reference_cuda` (the reference's own CUDA build against this engine's
+REF_DEM model on the reference-feasible stand-in: 20,000 x 20 beads on a
+1024 x 1024 grid with the reference's SRD, 2,621,440 solvent), `batch_256` and
+`adjoint_64x4k`.  Reference arm (--impl reference): the CPU port of the
+reference's step (oracle/, FP64, all host threads) on the same workload; it
+does not load libnwgb.
 
 Other workloads (--workload): wca_dense_2m (2M beads, no solvent),
 wca_small_4k (4k beads), batch_256 (256 uneven replicas in one launch per
@@ -36,6 +45,7 @@ REPO = Path(__file__).resolve().parent
 sys.path.insert(0, str(REPO / "nematic-worms_gb300"))
 
 GAP = 10
+REPEATS = 3
 PEAKS_FILE = REPO / "MEASURED_PEAKS.json"
 TRAFFIC_FILE = REPO / "profiles" / "traffic_per_unit.txt"
 FALLBACK_HBM_GBS = 6800.0
@@ -216,11 +226,25 @@ def cpu_baseline(cfg, pos, vel, budget_s: float = 20.0):
             "sample": sample, "seconds_per_step": per_step}
 
 
-def workload_config(name: str, seed: int):
-    from nwgb.init import baseline_config, initial_state
+def workload_config(name: str, seed: int, isolated: bool = False):
+    """Configuration and initial state of a single-system workload.  With
+    isolated, the configuration is derived in a child process, so that this
+    process never loads libnwgb (the reference arm)."""
+    from nwgb.init import initial_state
 
     w = WORKLOADS[name]
-    cfg = baseline_config(w["k"], seed=seed)
+    if isolated:
+        from nwgb.abi import NwConfig
+
+        code = ("import sys; sys.path.insert(0, %r); from nwgb.init import baseline_config; "
+                "sys.stdout.write(bytes(baseline_config(%d, seed=%d)).hex())" % (str(REPO / "nematic-worms_gb300"),
+                                                                                w["k"], seed))
+        out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, check=True).stdout
+        cfg = NwConfig.from_buffer_copy(bytes.fromhex(out.strip()))
+    else:
+        from nwgb.init import baseline_config
+
+        cfg = baseline_config(w["k"], seed=seed)
     pos, vel = initial_state(cfg, seed=seed, layout=w["layout"])
     return cfg, pos, vel
 
@@ -254,7 +278,7 @@ def run_reference(args):
         return 0
     import numpy as np
 
-    cfg, pos, vel = workload_config(args.workload, 0)
+    cfg, pos, vel = workload_config(args.workload, 0, isolated=True)
     sys.path.insert(0, str(REPO / "oracle"))
     import oracle as orc
 
@@ -289,6 +313,193 @@ def run_reference(args):
     return 0
 
 
+def schedule(first_step: int, steps: int, gap: int):
+    """Chunks of a K-step run starting at update first_step, aligned to whole
+    SRD periods: up to the next period boundary, whole periods, remainder."""
+    out = []
+    head = (-first_step) % gap
+    if head:
+        out.append(min(head, steps))
+    left = steps - sum(out)
+    out += [gap] * (left // gap)
+    if left % gap:
+        out.append(left % gap)
+    return out
+
+
+def run_steps(sysm, sched, dt):
+    launches = 0
+    for n in sched:
+        sysm.step(n, dt)
+        launches += sysm.last_launch_count
+    return launches
+
+
+def warm_and_prepare(sysm, cfg, warmup, steps, chunk):
+    """Exactly `warmup` steps, then capture (without running) every graph the
+    timed schedule replays.  Returns the schedule."""
+    done = 0
+    for n in schedule(0, warmup, chunk):
+        sysm.step(n, cfg.dt)
+        done += n
+    sched = schedule(done, steps, chunk)
+    at = done
+    for n in sched:
+        sysm.prepare(n, cfg.dt, at)
+        at += n
+    sysm.sync()
+    return sched
+
+
+def timed_region(sysm, sched, cfg, stream, dist=None):
+    """K steps between a barrier + synchronize on both sides, CUDA events on
+    the engine's stream.  Returns (ms, kernel launches)."""
+    import torch
+
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    launches = run_steps(sysm, sched, cfg.dt)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    return ev0.elapsed_time(ev1), launches
+
+
+def strategies_block(cfg, pos, vel, warmup, steps, stream):
+    """The same workload and start under each step strategy: the sorted scheme
+    (hash, stable sort and cell bounds every update, as the reference), capped
+    per-cell lists, and Verlet lists over those cells (the headline)."""
+    import nwgb
+    from nwgb import abi
+
+    out = {}
+    chunk = GAP if cfg.srd_enabled else 10
+    for name, strat in (("sorted", abi.NW_STRATEGY_SORTED), ("cell_lists", abi.NW_STRATEGY_CELL_LISTS),
+                        ("verlet", abi.NW_STRATEGY_VERLET)):
+        c = cfg.copy()
+        c.strategy = strat
+        with nwgb.System(c) as s:
+            s.set_stream(stream.cuda_stream)
+            s.set_array(abi.NW_POSITION, pos)
+            s.set_array(abi.NW_VELOCITY, vel)
+            s.zero_forces()
+            sched = warm_and_prepare(s, c, warmup, steps, chunk)
+            ms, launches = timed_region(s, sched, c, stream)
+            s.sync()
+        out[name] = {"ms_per_step": ms / steps, "value": c.n_beads * steps / (ms / 1e3), "steps": steps,
+                     "warmup": warmup, "launches_per_step": launches / steps}
+    return out
+
+
+R1 = dict(filaments=20000, filament_size=20, grid=(1024, 1024, 1))
+
+
+def r1_setters(p, s):
+    """main.cpp's setters for the stand-in run (flags -kbT=0.1 -gamma=2
+    -kBend=10 -kBond=57 -activity=0.5 -reverse=0 -boundX=0 -boundY=0
+    -boundZ=1, hardness at its default = the initial kBond 57.146436) and the
+    workload's bond rest length 0.8 (setBondSpringLength)."""
+    p.kbT = 0.1
+    s.kbT = 0.1
+    p.gamma = 2.0
+    p.bondBendingK = 10.0
+    p.bondSpringK = 57.0
+    p.activity = 0.5
+    p.reverseProbability = 0.0
+    p.spring = 57.146436
+    p.bondSpringL = 0.8
+    p.boundaryX, p.boundaryY, p.boundaryZ = 0, 0, 1
+
+
+def ref_dem_r1(warmup, steps, stream):
+    """This engine's REF_DEM model (the reference's collideFilaments
+    semantics) on the reference-feasible stand-in of the 400k + SRD workload,
+    from the reference's reset() state, through the handle API."""
+    import nwgb
+    from nwgb import abi
+    from nwgb.init import reference_reset
+
+    cfg = abi.default_config(abi.NW_MODEL_REF_DEM, R1["filaments"], R1["filament_size"], R1["grid"], True)
+    cfg.kT = cfg.srd_kT = 0.1
+    cfg.gamma = 2.0
+    cfg.bend_k = 10.0
+    cfg.bond_k = 57.0
+    cfg.activity = 0.5
+    cfg.reverse_probability = 0.0
+    cfg.spring = 57.146436
+    cfg.bond_r0 = 0.8
+    cfg.boundary[0], cfg.boundary[1], cfg.boundary[2] = abi.NW_PERIODIC, abi.NW_PERIODIC, abi.NW_WALL
+    cfg.dt = 0.005
+    pos, vel, tan = reference_reset(cfg)
+    with nwgb.System(cfg) as s:
+        s.set_stream(stream.cuda_stream)
+        s.set_array(abi.NW_POSITION, pos)
+        s.set_array(abi.NW_VELOCITY, vel)
+        s.set_array(abi.NW_TANGENT, tan)
+        s.zero_forces()
+        sched = warm_and_prepare(s, cfg, warmup, steps, int(cfg.srd_gap) * 2)
+        ms, launches = timed_region(s, sched, cfg, stream)
+        s.sync()
+    return {"ms_per_step": ms / steps, "value": cfg.n_beads * steps / (ms / 1e3), "steps": steps, "warmup": warmup,
+            "beads": cfg.n_beads, "solvent": cfg.n_solvent, "srd_gap": int(cfg.srd_gap), "launches_per_step":
+            launches / steps}
+
+
+def run_reference_cuda(args):
+    """The reference's own CUDA build (its kernels compiled for sm_103a from its
+    source, launched as its C-ABI layer does, thrust sort and cuRAND) running
+    its ParticleSystem::update loop on the stand-in configuration: W untimed
+    updates, then K updates between CUDA events on the legacy default stream.
+    Prints one JSON line; loads no part of this engine."""
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, str(REPO / "oracle"))
+    import ref_cuda
+
+    why = ref_cuda.available()
+    if why:
+        print(json.dumps({"impl": "reference_cuda", "unavailable": why}), flush=True)
+        return 0
+    rs = ref_cuda.RefSystem(reference=(R1["filaments"], R1["filament_size"], R1["grid"], True))
+    p, sv = rs.params, rs.solvent
+    r1_setters(p, sv)
+    rs.reset()
+    dt = 0.005
+    rs.run(args.warmup, dt)
+    ms = rs.run(args.steps, dt)
+    nb = rs.n_beads
+    line = {"impl": "reference_cuda", "metric": "bead-steps/s", "value": nb * args.steps / (ms / 1e3),
+            "unit": "bead-steps/s", "ms_per_step": ms / args.steps, "steps": args.steps, "warmup": args.warmup,
+            "config": {"workload": "ref_dem_r1", "beads": nb, "solvent": rs.n_solvent, "grid": list(R1["grid"]),
+                       "srd_gap": 5, "dt": dt}}
+    rs.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def reference_cuda_block(warmup, steps):
+    """Runs the reference CUDA arm in its own process (so that this process
+    never loads the reference build) and returns its line."""
+    cmd = [sys.executable, str(REPO / "bench.py"), "--impl", "reference_cuda", "--steps", str(steps), "--warmup",
+           str(warmup)]
+    env = dict(os.environ)
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        env.pop(k, None)
+    try:
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=900, env=env)
+        for line in r.stdout.splitlines()[::-1]:
+            if line.startswith("{"):
+                return json.loads(line)
+        return {"unavailable": "no output: " + (r.stderr.strip().splitlines() or ["?"])[-1][:300]}
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"{type(e).__name__}: {e}"[:300]}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -316,39 +527,26 @@ def run_ours(args):
     sysm.zero_forces()
 
     chunk = GAP if cfg.srd_enabled else 10
-    rem = args.steps % chunk
-    sched = [chunk] * (args.steps // chunk) + ([rem] if rem else [])
-    # warm-up: at least W steps in whole SRD periods, which captures the
-    # 10-step graph; a remainder graph is captured here as well
-    warm = 0
-    while warm < args.warmup:
-        sysm.step(chunk, cfg.dt)
-        warm += chunk
-    if rem:
-        sysm.step(rem, cfg.dt)
-        sysm.step(chunk - rem, cfg.dt)
-        warm += chunk
-    sysm.sync()
-
+    sched = warm_and_prepare(sysm, cfg, args.warmup, args.steps, chunk)
+    blob = sysm.checkpoint()
     clocks = ClockSampler(local)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
     clocks.start()
     time.sleep(0.3)  # let the sampler start before the timed region
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = []
     gpu_launches = 0
-    ev0.record(stream)
-    for n in sched:
-        sysm.step(n, cfg.dt)
-        gpu_launches += sysm.last_launch_count
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1)
+    for r in range(REPEATS):
+        if r:
+            sysm.restore(blob)  # the same start state for every repeat
+            at = sysm.step_index
+            for n in sched:
+                sysm.prepare(n, cfg.dt, at)
+                at += n
+            sysm.sync()
+        ms_r, gpu_launches = timed_region(sysm, sched, cfg, stream, dist)
+        reps.append(ms_r)
     clk = clocks.stop()
-    if dist:
-        dist.barrier()
     sysm.sync()
+    ms = statistics.median(reps)
     value, ms_max = job_rate(dist, ms, nb * args.steps, device="cuda")
 
     # ---- end to end through the C ABI with host buffers ------------------------------
@@ -400,26 +598,50 @@ def run_ours(args):
                          "note": "whole step (timed value) against the same peak"},
                 "kernel_share": {k: round(v[0] / total_prof, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
                 "kernel_avg_ms": {k: round(v[0] / v[1], 5) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}}
+    sysm.close()
 
+    line = None
     if rank == 0:
         line = {"metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": world,
-                "steps": args.steps, "warmup": warm, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": config_block(args.workload, cfg, world), "clocks": clk,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": config_block(args.workload, cfg, world), "clocks": clk,
+                "timing": {"repeats": REPEATS, "ms_per_step": [t / args.steps for t in reps],
+                           "median_ms_per_step": ms / args.steps, "spread": (max(reps) - min(reps)) / ms,
+                           "note": "each repeat restarts from the checkpoint taken after the warm-up"},
                 "e2e": {"value": e2e_value, "unit": "bead-steps/s", "h2d_bytes_per_step": nb * 32,
                         "d2h_bytes_per_step": nb * 32, "steps": e2e_steps,
                         "path": "nw_set_array(pos, vel) + nw_step(1) + nw_get_array(pos, vel) per step, pinned host"},
                 "gpu_launches": gpu_launches, "roofline": roofline}
+        if world == 1 and not args.no_extras:
+            k_sub = min(args.steps, 1000)
+            line["strategies"] = strategies_block(cfg, pos, vel, args.warmup, k_sub, stream)
+            if args.workload == "wca_srd_400k":
+                k_ref = min(args.steps, 200)
+                ours = ref_dem_r1(args.warmup, k_ref, stream)
+                theirs = reference_cuda_block(args.warmup, k_ref)
+                blk = {"ours_ref_dem": ours, "reference": theirs}
+                if "ms_per_step" in theirs:
+                    blk["speedup"] = theirs["ms_per_step"] / ours["ms_per_step"]
+                line["reference_cuda"] = blk
+                line["batch_256"] = batch_block(args, steps=min(args.steps, 1000))
+                line["adjoint_64x4k"] = adjoint_block(args)
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(cfg, pos.astype(np.float64), vel.astype(np.float64))
         print(json.dumps(line), flush=True)
-    sysm.close()
     if dist:
         dist.destroy_process_group()
     return 0
 
 
 def run_batch(args):
+    line = batch_block(args)
+    if env_rank()[0] == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def batch_block(args, steps=None):
     """Batched replicas: every step of all replicas in one launch, CUDA graphs of
     100 steps, launch shape and neighbour search from the autotuner.  Reported
     beside it: the same replicas run one by one through the single-system step
@@ -434,14 +656,14 @@ def run_batch(args):
 
     rank, world, local = env_rank()
     torch.cuda.set_device(local)
-    R = WORKLOADS[args.workload]["batch"]
+    R = WORKLOADS["batch_256"]["batch"]
     cfgs = batch_configs(R, seed=1000 * rank)
     states = [initial_state(c, seed=r, layout="rows") for r, c in enumerate(cfgs)]
     total = sum(c.n_beads for c in cfgs)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     chunk = 100
-    nchunks = max(1, args.steps // chunk)
+    nchunks = max(1, (args.steps if steps is None else steps) // chunk)
 
     def timed(step_fn, n):
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -506,7 +728,7 @@ def run_batch(args):
     line = {"metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": world,
             "steps": chunk * nchunks, "warmup": warm, "ms_per_step": ms / (chunk * nchunks),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, "replicas": R, "beads": total, "model": "WCA_WORMS",
+            "config": {"workload": "batch_256", "replicas": R, "beads": total, "model": "WCA_WORMS",
                        "graph_steps": chunk, "parallelism": f"replicas x{world}",
                        "tuning": {"threads_per_block": tune.threads_per_block, "strategy": int(tune.strategy),
                                   "neighbor_skin": round(float(tune.neighbor_skin), 3),
@@ -518,12 +740,17 @@ def run_batch(args):
             "plain": {"value": plain_value, "beads": pc.n_beads, "box": side,
                       "path": "one single system of the same bead count (20-bead worms, packing 0.45)"},
             "batched_over_plain": value / plain_value, "batched_over_sequential": value / seq_value}
-    if rank == 0:
+    return line
+
+
+def run_adjoint(args):
+    line = adjoint_block(args)
+    if env_rank()[0] == 0:
         print(json.dumps(line), flush=True)
     return 0
 
 
-def run_adjoint(args):
+def adjoint_block(args):
     """Differentiable rollout: forward + adjoint of 200 steps for 64 replicas of
     the 4k-bead workload (FP32), timed on the device; beside it the production
     batched step on the same replicas and steps."""
@@ -538,7 +765,7 @@ def run_adjoint(args):
 
     rank, world, local = env_rank()
     torch.cuda.set_device(local)
-    R = WORKLOADS[args.workload]["adjoint"]
+    R = WORKLOADS["adjoint_64x4k"]["adjoint"]
     H, SEG = 200, 20
     cfg = baseline_config(0, seed=7)
     states = [initial_state(cfg, seed=r, layout="patches") for r in range(R)]
@@ -587,16 +814,14 @@ def run_adjoint(args):
     line = {"metric": "bead-steps/s", "value": nbt * H / ((f_ms + b_ms) / 1e3), "unit": "bead-steps/s",
             "n_gpus": world, "steps": H * len(fwd), "warmup": args.warmup, "ms_per_step": (f_ms + b_ms) / H,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, "replicas": R, "beads": nbt, "horizon": H, "segment": SEG,
+            "config": {"workload": "adjoint_64x4k", "replicas": R, "beads": nbt, "horizon": H, "segment": SEG,
                        "loss": "(S2 - 0.7)^2 + |C_v - C_target|^2, 32 bins"},
             "adjoint": {"forward_ms": f_ms, "backward_ms": b_ms, "backward_over_forward": b_ms / f_ms,
                         "gradient_over_production_step": (f_ms + b_ms) / prod_ms,
                         "production_batched_ms": prod_ms,
                         "note": "forward = the rollout's own frozen-list step (with checkpoints); "
                                 "production = the batched engine over the same replicas and steps"}}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def defect_frame(n_worms, L, box, seed=11):
@@ -710,12 +935,16 @@ def main():
     # keeps warming and longer runs measure a different, hotter system
     ap.add_argument("--steps", type=int, default=10000)
     ap.add_argument("--warmup", type=int, default=100)
-    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--impl", choices=["ours", "reference", "reference_cuda"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="wca_srd_400k")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the strategies / reference_cuda / batch / "
+                    "adjoint sub-blocks of the default line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.impl == "reference_cuda":
+        return run_reference_cuda(args)
     if "adjoint" in WORKLOADS[args.workload]:
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no gradients"}), flush=True)

@@ -210,6 +210,14 @@ nw_status nw_config_default(NwConfig* cfg, int model, uint32_t num_filaments,
 /* Re-derive box/origin/cell fields after the caller changed grid or cell size
  * (origin = -box/2 as in simulation/particleSystem.cpp:76-79). */
 nw_status nw_config_finalize(NwConfig* cfg);
+/* Replaces: ParticleSystem::reset (simulation/particleSystem.cpp:583-678).
+ * The reference's initial state for cfg into host arrays of (beads + solvent)
+ * x 4 floats (pos, vel) and beads x 4 floats (tan): filaments along x on a
+ * lattice of bond_r0 spacing, every other one (by draw) reversed, bead
+ * velocities 0.1 U(-1, 1), solvent uniform in the box with velocities
+ * 5 U(-1, 1), all drawn from the C library's rand() after srand(1) (the
+ * reference never seeds it).  Host only; resets rand()'s state. */
+nw_status nw_reference_reset(const NwConfig* cfg, float* pos, float* vel, float* tan);
 
 /* Check a configuration without creating anything. */
 nw_status nw_config_validate(const NwConfig* cfg);
@@ -257,6 +265,11 @@ nw_status nw_zero_forces(nw_system* sys);
  * nsteps times with step size dt (dt <= 0 uses cfg.dt).  Asynchronous on the
  * system's stream; runs from a cached CUDA graph when nsteps > 1. */
 nw_status nw_step(nw_system* sys, int nsteps, float dt);
+/* Capture, without running anything, the CUDA graph that nw_step(sys, nsteps,
+ * dt) replays when called at update index first_step (only its SRD phase
+ * matters), so that a later nw_step pays no capture.  No counterpart in the
+ * reference; a no-op when graphs are off. */
+nw_status nw_step_prepare(nw_system* sys, int nsteps, float dt, uint64_t first_step);
 /* Wait for the stream, then report and clear the device error word. */
 nw_status nw_sync(nw_system* sys);
 nw_status nw_error_word(nw_system* sys, uint32_t* flags);

@@ -1,6 +1,7 @@
 // nw_config.cpp — configuration defaults, derivation and validation of the
 // C ABI (include/nwgb.h).  Host code only.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "../../include/nwgb.h"
@@ -24,6 +25,63 @@ nw_status nw_config_finalize(NwConfig* c)
     for (int a = 0; a < 3; ++a) {
         c->box[a] = (float)c->grid[a] * c->cell_size[a];
         c->origin[a] = -c->box[a] / 2.0f;
+    }
+    return NW_OK;
+}
+
+nw_status nw_reference_reset(const NwConfig* c, float* pos, float* vel, float* tan)
+{
+    if (!c || !pos || !vel || !tan) return NW_ERR_INVALID;
+    const uint32_t L = c->filament_size, M = c->num_filaments;
+    const uint64_t nb = (uint64_t)M * L;
+    const uint64_t ns = c->srd_enabled ? c->num_solvent : 0;
+    const float R = c->radius, bl = c->bond_r0;
+    const float flen = (float)L * bl + 2.0f * R;
+    const long xdim = (long)std::floor(c->box[0] / flen);
+    const long ydim = (long)std::floor(c->box[1] / (2.0f * R));
+    if (nb && (xdim <= 0 || ydim <= 0)) return NW_ERR_INVALID;
+    const long plane = xdim * ydim;
+    srand(1);
+    auto frand = []() { return (float)rand() / (float)RAND_MAX; };
+    for (uint64_t i = 0; i < nb; ++i) {
+        const long w = (long)(i / L);
+        const float x = ((float)(w % xdim) * flen + R) + (float)(i % L) * bl;
+        const float y = 2.0f * R * (float)((w / xdim) % ydim + 1);
+        const float z = 2.0f * R * (float)(w / plane + 1);
+        float* p = pos + 4 * i;
+        p[0] = x + c->origin[0];
+        p[1] = y + c->origin[1];
+        p[2] = z + c->origin[2];
+        p[3] = R;
+        float* v = vel + 4 * i;
+        for (int a = 0; a < 3; ++a) v[a] = 0.1f * (frand() * 2.0f - 1.0f);
+        v[3] = c->mass;
+        float* t = tan + 4 * i;
+        t[0] = 1.0f;
+        t[1] = t[2] = t[3] = 0.0f;
+    }
+    for (uint32_t w = 0; w < M; ++w) {
+        if (frand() < 0.5f) continue;
+        for (uint32_t p = 0; p < L / 2; ++p) {
+            const uint64_t i = (uint64_t)w * L + p, j = (uint64_t)(w + 1) * L - 1 - p;
+            for (int a = 0; a < 4; ++a) {
+                float tmp = pos[4 * i + a];
+                pos[4 * i + a] = pos[4 * j + a];
+                pos[4 * j + a] = tmp;
+            }
+            for (int a = 0; a < 4; ++a) {
+                tan[4 * i + a] = -tan[4 * i + a];
+                tan[4 * j + a] = -tan[4 * j + a];
+            }
+        }
+    }
+    for (uint64_t s = 0; s < ns; ++s) {
+        float* p = pos + 4 * (nb + s);
+        for (int a = 0; a < 3; ++a) p[a] = c->box[a] * frand() + c->origin[a];
+        p[3] = 0.0f;
+        float* v = vel + 4 * (nb + s);
+        for (int a = 0; a < 3; ++a) v[a] = 5.0f * (frand() * 2.0f - 1.0f);
+        v[3] = c->solvent_mass;
     }
     return NW_OK;
 }

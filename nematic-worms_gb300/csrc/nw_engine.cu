@@ -824,6 +824,46 @@ nw_status nw_zero_forces(nw_system* s)
     return cuda_status(e);
 }
 
+// The cached graph of nsteps updates from an update index of the given SRD
+// phase, captured on first use.  A graph depends on the host state only
+// through the phase (which updates collide); buffers are picked on the device
+// from the step counter.
+static cudaError_t find_graph(nw_system* s, int nsteps, float dt, uint64_t first_step, GraphEntry** out)
+{
+    const uint32_t phase = s->cfg.srd_enabled ? (uint32_t)(first_step % s->cfg.srd_gap) : 0u;
+    uint32_t bits;
+    std::memcpy(&bits, &dt, 4);
+    for (auto& g : s->graphs)
+        if (g.nsteps == nsteps && g.dt_bits == bits && g.phase == phase && g.version == s->version) {
+            *out = &g;
+            return cudaSuccess;
+        }
+    if (s->graphs.size() >= 24) drop_graphs(s);  // single steps take one graph per collision phase
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    uint64_t launches = enqueue_steps(s, nsteps, dt, first_step);
+    e = cudaStreamEndCapture(s->stream, &graph);
+    if (e != cudaSuccess) return e;
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return e;
+    s->graphs.push_back({nsteps, bits, phase, s->version, exec, launches});
+    *out = &s->graphs.back();
+    return cudaSuccess;
+}
+
+nw_status nw_step_prepare(nw_system* s, int nsteps, float dt, uint64_t first_step)
+{
+    if (!s || nsteps < 0) return NW_ERR_INVALID;
+    if (nsteps == 0 || !s->use_graphs) return NW_OK;
+    if (!(dt > 0.0f)) dt = s->cfg.dt;
+    if (!std::isfinite(dt)) return NW_ERR_INVALID;
+    GraphEntry* g = nullptr;
+    return cuda_status(find_graph(s, nsteps, dt, first_step, &g));
+}
+
 nw_status nw_step(nw_system* s, int nsteps, float dt)
 {
     if (!s || nsteps < 0) return NW_ERR_INVALID;
@@ -832,28 +872,10 @@ nw_status nw_step(nw_system* s, int nsteps, float dt)
     if (!std::isfinite(dt)) return NW_ERR_INVALID;
     cudaError_t e = clean_lists(s);
     if (e != cudaSuccess) return cuda_status(e);
-    const uint32_t phase = s->cfg.srd_enabled ? (uint32_t)(s->step % s->cfg.srd_gap) : 0u;
     if (s->use_graphs) {
-        uint32_t bits;
-        std::memcpy(&bits, &dt, 4);
         GraphEntry* hit = nullptr;
-        for (auto& g : s->graphs)
-            if (g.nsteps == nsteps && g.dt_bits == bits && g.phase == phase && g.version == s->version) hit = &g;
-        if (!hit) {
-            if (s->graphs.size() >= 24) drop_graphs(s);  // single steps take one graph per collision phase
-            cudaGraph_t graph = nullptr;
-            e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
-            if (e != cudaSuccess) return cuda_status(e);
-            uint64_t launches = enqueue_steps(s, nsteps, dt, s->step);
-            e = cudaStreamEndCapture(s->stream, &graph);
-            if (e != cudaSuccess) return cuda_status(e);
-            cudaGraphExec_t exec = nullptr;
-            e = cudaGraphInstantiate(&exec, graph, 0);
-            cudaGraphDestroy(graph);
-            if (e != cudaSuccess) return cuda_status(e);
-            s->graphs.push_back({nsteps, bits, phase, s->version, exec, launches});
-            hit = &s->graphs.back();
-        }
+        e = find_graph(s, nsteps, dt, s->step, &hit);
+        if (e != cudaSuccess) return cuda_status(e);
         e = cudaGraphLaunch(hit->exec, s->stream);
         s->last_launches = hit->launches;
     } else {

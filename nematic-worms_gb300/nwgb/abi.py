@@ -201,6 +201,8 @@ HANDLE_API = [
     ("nw_device_array", C.c_int, [_sysp, C.c_int, C.POINTER(_P)]),
     ("nw_zero_forces", C.c_int, [_sysp]),
     ("nw_step", C.c_int, [_sysp, C.c_int, _f32]),
+    ("nw_step_prepare", C.c_int, [_sysp, C.c_int, _f32, C.c_uint64]),
+    ("nw_reference_reset", C.c_int, [C.POINTER(NwConfig), _P, _P, _P]),
     ("nw_sync", C.c_int, [_sysp]),
     ("nw_error_word", C.c_int, [_sysp, C.POINTER(_u32)]),
     ("nw_get_step", C.c_int, [_sysp, C.POINTER(C.c_uint64)]),

@@ -13,7 +13,6 @@ drawing from the C library's rand() exactly as the reference does.
 from __future__ import annotations
 
 import ctypes as C
-import ctypes.util
 import math
 
 import numpy as np
@@ -247,61 +246,17 @@ def initial_state(cfg: NwConfig, seed: int = 0, layout: str = "patches"):
     return pos, vel
 
 
-def reference_reset(cfg: NwConfig):
+def reference_reset(cfg: NwConfig, lib=None):
     """The reference's reset() (simulation/particleSystem.cpp:583-678):
     filaments on a lattice along x with spacing bondSpringL, half of them
     flipped, velocities 0.1 * U(-1, 1), solvent uniform with speed scale 5,
-    all drawn from the C library's unseeded rand() stream."""
-    libc = C.CDLL(ctypes.util.find_library("c"))
-    libc.rand.restype = C.c_int
-    libc.srand(1)
-    RAND_MAX = 2147483647.0
-
-    def frand():
-        return np.float32(libc.rand()) / np.float32(RAND_MAX)
-
+    all drawn from the C library's rand() after srand(1) (nw_reference_reset
+    in libnwgb).  Returns (pos, vel, tan) as float32 arrays."""
+    lib = lib or abi.load_library()
     nb, ns = cfg.n_beads, cfg.n_solvent
-    L, M = int(cfg.filament_size), int(cfg.num_filaments)
-    R = np.float32(cfg.radius)
-    bl = np.float32(cfg.bond_r0)
-    box = np.array(cfg.box, dtype=np.float32)
-    org = np.array(cfg.origin, dtype=np.float32)
-    flen = np.float32(np.float32(L) * bl + np.float32(2.0) * R)
-    xdim = int(math.floor(box[0] / flen))
-    ydim = int(math.floor(box[1] / (2 * R)))
-    plane = xdim * ydim
     pos = np.zeros((nb + ns, 4), dtype=np.float32)
     vel = np.zeros((nb + ns, 4), dtype=np.float32)
-    tan = np.zeros((nb, 4), dtype=np.float32)
-    for i in range(nb):
-        w = i // L
-        x_head = np.float32(w % xdim) * flen + R
-        x = x_head + np.float32(i % L) * bl
-        y = np.float32(2.0) * R * np.float32((w // xdim) % ydim + 1)
-        z = np.float32(2.0) * R * np.float32(w // plane + 1)
-        pos[i] = (x + org[0], y + org[1], z + org[2], R)
-        vel[i, 0] = np.float32(0.1) * (frand() * np.float32(2.0) - np.float32(1.0))
-        vel[i, 1] = np.float32(0.1) * (frand() * np.float32(2.0) - np.float32(1.0))
-        vel[i, 2] = np.float32(0.1) * (frand() * np.float32(2.0) - np.float32(1.0))
-        vel[i, 3] = cfg.mass
-        tan[i] = (1.0, 0.0, 0.0, 0.0)
-    for w in range(M):
-        if frand() < np.float32(0.5):
-            continue
-        for p in range(L // 2):
-            i, j = w * L + p, (w + 1) * L - 1 - p
-            pos[[i, j]] = pos[[j, i]]
-            tan[i] = -tan[i]
-            tan[j] = -tan[j]
-    for s in range(ns):
-        i = nb + s
-        pos[i, 0] = box[0] * frand() + org[0]
-        pos[i, 1] = box[1] * frand() + org[1]
-        pos[i, 2] = box[2] * frand() + org[2]
-        pos[i, 3] = 0.0
-        v0 = np.float32(5.0)
-        vel[i, 0] = v0 * (frand() * np.float32(2.0) - np.float32(1.0))
-        vel[i, 1] = v0 * (frand() * np.float32(2.0) - np.float32(1.0))
-        vel[i, 2] = v0 * (frand() * np.float32(2.0) - np.float32(1.0))
-        vel[i, 3] = cfg.solvent_mass
-    return pos, vel, tan
+    tan = np.zeros((max(nb, 1), 4), dtype=np.float32)
+    abi.check(lib.nw_reference_reset(C.byref(cfg), pos.ctypes.data, vel.ctypes.data, tan.ctypes.data),
+              "nw_reference_reset")
+    return pos, vel, tan[:nb]

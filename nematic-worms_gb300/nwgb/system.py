@@ -110,6 +110,12 @@ class System:
     def step(self, n: int = 1, dt: float = 0.0) -> None:
         check(self.lib.nw_step(self._h, int(n), float(dt)), "nw_step")
 
+    def prepare(self, n: int, dt: float = 0.0, first_step: int | None = None) -> None:
+        """Capture the graph that step(n, dt) replays from update first_step
+        (default: the current one) without running it."""
+        fs = self.step_index if first_step is None else int(first_step)
+        check(self.lib.nw_step_prepare(self._h, int(n), float(dt), fs), "nw_step_prepare")
+
     def sync(self) -> None:
         check(self.lib.nw_sync(self._h), "nw_sync")
 
@@ -228,6 +234,17 @@ class ParticleSystem:
             self._sys.set_config(self._cfg)
             self._dirty = False
         self._sys.step(1, deltaTime)
+
+    def reset(self) -> None:
+        """ParticleSystem::reset (simulation/particleSystem.cpp:583-678): the
+        reference's lattice state, drawn from rand() after srand(1)."""
+        from .init import reference_reset
+
+        pos, vel, tan = reference_reset(self._cfg)
+        self._sys.set_array(abi.NW_POSITION, pos)
+        self._sys.set_array(abi.NW_VELOCITY, vel)
+        self._sys.set_array(abi.NW_TANGENT, tan)
+        self._sys.zero_forces()
 
     def getArray(self, array: int) -> np.ndarray:
         """Bead data (n_beads x 4 floats), like the reference's getArray."""

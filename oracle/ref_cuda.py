@@ -57,6 +57,8 @@ _SIGS = {
     "nwref_solventCellCentorOfMomentum": [_P, _P, _P, _P, _P, _u],
     "nwref_solventIsokineticThermostat": [_P, _P, _P, _P, _P, _u],
     "nwref_create": [_P, _P, _u],
+    "nwref_create_reference": [_u, _u, _u, _u, _u, C.c_int],
+    "nwref_reset": [_P],
     "nwref_destroy": [_P],
     "nwref_params": [_P],
     "nwref_solvent": [_P],
@@ -68,7 +70,7 @@ _SIGS = {
     "nwref_run": [_P, _u, _f, C.POINTER(_f)],
     "nwref_sync": [],
 }
-_RESTYPES = {"nwref_create": _P, "nwref_params": C.POINTER(SimParams), "nwref_solvent": C.POINTER(SolventParams),
+_RESTYPES = {"nwref_create": _P, "nwref_create_reference": _P, "nwref_params": C.POINTER(SimParams), "nwref_solvent": C.POINTER(SolventParams),
              "nwref_buffer": _P, "nwref_buffer_bytes": C.c_size_t, "nwref_update_count": C.c_ulonglong,
              "nwref_destroy": None, "nwref_error": C.c_char_p}
 
@@ -138,13 +140,24 @@ class RefSystem:
     """The reference's ParticleSystem buffers (particleSystem.cpp:172-223) and
     update() / _solventUpdate() sequence (:249-413) on the reference kernels."""
 
-    def __init__(self, params: SimParams, solvent: SolventParams | None = None, solvent_gap: int = 5):
+    def __init__(self, params: SimParams | None = None, solvent: SolventParams | None = None, solvent_gap: int = 5,
+                 reference=None):
+        """From parameter blocks, or with reference=(numFilaments, filamentSize,
+        (gx, gy, gz), srd) as the reference's constructor builds them."""
         L = lib()
-        self._h = L.nwref_create(C.byref(params), C.byref(solvent) if solvent is not None else None, solvent_gap)
+        if reference is not None:
+            M, Lf, g, srd = reference
+            self._h = L.nwref_create_reference(M, Lf, g[0], g[1], g[2], 1 if srd else 0)
+        else:
+            self._h = L.nwref_create(C.byref(params), C.byref(solvent) if solvent is not None else None, solvent_gap)
         if not self._h:
             raise RefCudaError(L.nwref_error().decode())
-        self.n_beads = int(params.numParticles)
-        self.n_solvent = int(solvent.numParticles) if solvent is not None and solvent.enabled else 0
+        self.n_beads = int(self.params.numParticles)
+        self.n_solvent = int(self.solvent.numParticles) if self.solvent.enabled else 0
+
+    def reset(self) -> None:
+        """ParticleSystem::reset: the reference's lattice state, uploaded."""
+        check(lib().nwref_reset(self._h))
 
     @property
     def params(self) -> SimParams:

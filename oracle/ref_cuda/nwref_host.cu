@@ -265,6 +265,9 @@ int nwref_solventIsokineticThermostat(float* vel, float* sortedVel, uint* cellSt
 
 /* ---- the reference's ParticleSystem buffers and update sequence ----------- */
 
+struct nwref_system;
+int nwref_copy(nwref_system* sys, int which, void* host, size_t offset, size_t bytes, int to_device);
+
 enum {
     NWREF_POS, NWREF_VEL, NWREF_TANGENT, NWREF_FORCE, NWREF_FORCE_OLD, NWREF_RANDOM, NWREF_SORTED_POS,
     NWREF_SORTED_VEL, NWREF_SORTED_TANGENT, NWREF_HASH, NWREF_INDEX, NWREF_CELL_START, NWREF_CELL_END,
@@ -326,6 +329,117 @@ nwref_system* nwref_create(const SimParams* p, const SolventParams* s, uint solv
     if (sys->srd && nwref_setSolventParameters(&sys->solvent)) return nullptr;
     if (nwref_setParameters(&sys->params)) return nullptr;
     return sys;
+}
+
+/* ParticleSystem(numFilaments, filamentSize, gridSize, srd): the
+ * constructor's parameter defaults (particleSystem.cpp:64-107), the SRD
+ * parameters of _initSolventParams (:124-148: SRD cells of two bead cells,
+ * 10 solvent per SRD cell, a collision every 5 updates) and the buffers of
+ * _initialize.  The caller applies the setters main.cpp would
+ * (nwref_params / nwref_solvent) before the first update. */
+nwref_system* nwref_create_reference(uint numFilaments, uint filamentSize, uint gx, uint gy, uint gz, int srd)
+{
+    SimParams p;
+    memset(&p, 0, sizeof p);
+    p.numFilaments = numFilaments;
+    p.filamentSize = filamentSize;
+    p.numParticles = numFilaments * filamentSize;
+    p.particleRadius = 0.5f;
+    p.particleMass = 1.0f;
+    p.gridSize = make_uint3(gx, gy, gz);
+    p.numCells = gx * gy * gz;
+    const float cell = p.particleRadius * 2.0f;
+    p.cellSize = make_float3(cell, cell, cell);
+    p.boxSize = make_float3(gx * cell, gy * cell, gz * cell);
+    p.origin = make_float3(-p.boxSize.x / 2.0f, -p.boxSize.y / 2.0f, -p.boxSize.z / 2.0f);
+    p.boundaryX = p.boundaryY = p.boundaryZ = PERIODIC;
+    p.bondSpringK = 57.f;
+    p.bondSpringL = p.particleRadius * 0.8f;
+    p.bondBendingK = 0.001f;
+    p.spring = 0.5f;
+    p.damping = 0.02f;
+    p.shear = 0.1f;
+    p.attraction = 0.0f;
+    p.boundaryDamping = -0.5f;
+    p.activity = 0.1f;
+    p.reverseProbability = 0.0f;
+    p.kbT = 1.0f;
+    p.gamma = 0.01f;
+    p.gravity = make_float3(0.f, 0.f, 0.f);
+    SolventParams sv;
+    memset(&sv, 0, sizeof sv);
+    if (srd) {
+        sv.enabled = true;
+        sv.alpha = 2.26893f;
+        sv.gridSize = make_uint3(gx / 2, gy / 2, gz / 2 > 1 ? gz / 2 : 1);
+        sv.cellSize = make_float3(2.0f * cell, 2.0f * cell, 2.0f * cell);
+        sv.numCells = sv.gridSize.x * sv.gridSize.y * sv.gridSize.z;
+        sv.randOffset = make_float3(0.f, 0.f, 0.f);
+        sv.particleMass = 1.0f;
+        sv.kbT = p.kbT;
+        sv.numParticles = (uint)(10.0f * (float)sv.numCells);
+    }
+    return nwref_create(&p, srd ? &sv : nullptr, 5);
+}
+
+/* ParticleSystem::reset (particleSystem.cpp:583-678): filaments along x on
+ * the lattice, every one whose draw is >= 0.5 reversed, solvent uniform in
+ * the box; rand() after srand(1) (the reference never seeds it).  Uploads
+ * positions and velocities of beads and solvent and the bead tangents. */
+int nwref_reset(nwref_system* sys)
+{
+    const SimParams& P = sys->params;
+    const uint L = P.filamentSize, nb = sys->numParticles, ns = sys->numSolvent;
+    const float R = P.particleRadius;
+    const float flen = (float)L * P.bondSpringL + 2.0f * R;
+    const int xdim = (int)floorf(P.boxSize.x / flen);
+    const int ydim = (int)floorf(P.boxSize.y / (2 * R));
+    if (nb && (xdim <= 0 || ydim <= 0)) return fail("box too small for the reset lattice", -5);
+    const uint plane = (uint)(xdim * ydim);
+    float* pos = (float*)calloc(4 * (size_t)(nb + ns), sizeof(float));
+    float* vel = (float*)calloc(4 * (size_t)(nb + ns), sizeof(float));
+    float* tan = (float*)calloc(4 * (size_t)(nb ? nb : 1), sizeof(float));
+    srand(1);
+    auto frand = []() { return rand() / (float)RAND_MAX; };
+    for (uint i = 0; i < nb; ++i) {
+        const uint w = i / L;
+        const float xh = (float)(w % (uint)xdim) * flen + R;
+        pos[4 * i + 0] = xh + (float)(i % L) * P.bondSpringL + P.origin.x;
+        pos[4 * i + 1] = 2.f * R * (float)((w / (uint)xdim) % (uint)ydim + 1) + P.origin.y;
+        pos[4 * i + 2] = 2.f * R * (float)(w / plane + 1) + P.origin.z;
+        pos[4 * i + 3] = R;
+        for (int a = 0; a < 3; ++a) vel[4 * i + a] = 0.1f * (frand() * 2.0f - 1.0f);
+        vel[4 * i + 3] = P.particleMass;
+        tan[4 * i] = 1.0f;
+    }
+    for (uint w = 0; w < P.numFilaments; ++w) {
+        if (frand() < 0.5f) continue;
+        for (uint q = 0; q < L / 2; ++q) {
+            const size_t i = (size_t)w * L + q, j = (size_t)(w + 1) * L - 1 - q;
+            for (int a = 0; a < 4; ++a) {
+                const float t = pos[4 * i + a];
+                pos[4 * i + a] = pos[4 * j + a];
+                pos[4 * j + a] = t;
+                tan[4 * i + a] = -tan[4 * i + a];
+                tan[4 * j + a] = -tan[4 * j + a];
+            }
+        }
+    }
+    for (uint k = 0; k < ns; ++k) {
+        const size_t i = (size_t)nb + k;
+        pos[4 * i + 0] = P.boxSize.x * frand() + P.origin.x;
+        pos[4 * i + 1] = P.boxSize.y * frand() + P.origin.y;
+        pos[4 * i + 2] = P.boxSize.z * frand() + P.origin.z;
+        for (int a = 0; a < 3; ++a) vel[4 * i + a] = 5.0f * (frand() * 2.0f - 1.0f);
+        vel[4 * i + 3] = sys->solvent.particleMass;
+    }
+    int st = nwref_copy(sys, NWREF_POS, pos, 0, 16 * (size_t)(nb + ns), 1);
+    if (!st) st = nwref_copy(sys, NWREF_VEL, vel, 0, 16 * (size_t)(nb + ns), 1);
+    if (!st && nb) st = nwref_copy(sys, NWREF_TANGENT, tan, 0, 16 * (size_t)nb, 1);
+    free(pos);
+    free(vel);
+    free(tan);
+    return st;
 }
 
 void nwref_destroy(nwref_system* sys)
