@@ -88,7 +88,11 @@ void sortParticles(uint* dGridParticleHash, uint* dGridParticleIndex, uint numPa
  * At most 262,144 keys: larger counts return NW_ERR_INVALID (2) and leave
  * the arrays untouched.  Returns an nw_status (0 = OK).  The first call on a
  * device looks up the array's device address, so make that first call before
- * any stream capture.  All calls share the one array; calls that overlap on
+ * any stream capture (a first call inside capture returns NW_ERR_INVALID);
+ * calls outside capture look it up again, so after a cudaDeviceReset make one
+ * call outside capture before capturing again.  A CUDA error already pending
+ * from earlier work is returned as NW_ERR_CUDA before anything is launched
+ * and left pending.  All calls share the one array; calls that overlap on
  * the GPU race.  Runs on the legacy default stream, like sortParticles. */
 int nw_sort_particles_noalloc(uint* dGridParticleHash, uint* dGridParticleIndex, uint numParticles);
 /* particleSystem_cuda.cu:284-306 — random filament reversal. */

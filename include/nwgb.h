@@ -165,8 +165,10 @@ typedef struct NwConfig {
  *              every pair within lj_rcut is on them, and rebuild them in the
  *              pair pass otherwise.  Same forces as CELL_LISTS up to the
  *              order of the FP32 sums.
- *  AUTO        VERLET for WCA_WORMS, CELL_LISTS for REF_DEM (whose pair set
- *              is all beads of the neighbour cells, not a radius). */
+ *  AUTO        VERLET for WCA_WORMS, SORTED for REF_DEM (whose pair set is
+ *              all beads of the neighbour cells, not a radius; its sorted
+ *              pair pass on a single z layer runs cell-tiled in shared
+ *              memory). */
 typedef enum {
     NW_STRATEGY_AUTO = 0,
     NW_STRATEGY_SORTED = 1,

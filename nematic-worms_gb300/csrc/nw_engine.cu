@@ -152,7 +152,12 @@ uint64_t enqueue_bead_step(const DevParams& P, const StepBuffers& B, uint32_t nc
         NW_MARK("stable_gather");
         stable_gather_kernel<true><<<cdiv(P.nb, 256), 256, 0, s>>>(P, B);
         NW_MARK("pair_ref");
-        pair_ref_kernel<<<cdiv(P.nb, 256), 256, 0, s>>>(P, B);
+        if (P.grid[2] == 1u) {
+            const uint32_t tiles = cdiv(P.grid[0], kRefTX) * cdiv(P.grid[1], kRefTY);
+            pair_ref_tiled_kernel<<<tiles, kRefThreads, kRefSmem, s>>>(P, B);
+        } else {
+            pair_ref_kernel<<<cdiv(P.nb, 256), 256, 0, s>>>(P, B);
+        }
     } else {
         NW_MARK("stable_gather");
         stable_gather_kernel<false><<<cdiv(P.nb, 256), 256, 0, s>>>(P, B);
@@ -558,6 +563,14 @@ nw_status nw_create(const NwConfig* cfg, nw_system** out)
         return NW_ERR_CUDA;
     }
     s->stream = s->own_stream;
+    // the cell-tiled REF_DEM pair pass stages more than the default 48 KB
+    if (cudaFuncSetAttribute(pair_ref_tiled_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRefSmem) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        cudaStreamDestroy(s->own_stream);
+        delete s;
+        return NW_ERR_CUDA;
+    }
     s->lists = effective_strategy(*cfg) != NW_STRATEGY_SORTED;
     const DevParams P0 = make_dev_params(*cfg, cfg->dt);
     s->vl = P0.vl_on != 0;

@@ -25,7 +25,7 @@ struct Prof {
 inline int effective_strategy(const NwConfig& c)
 {
     if (c.strategy != NW_STRATEGY_AUTO) return c.strategy;
-    return c.model == NW_MODEL_WCA_WORMS ? NW_STRATEGY_VERLET : NW_STRATEGY_CELL_LISTS;
+    return c.model == NW_MODEL_WCA_WORMS ? NW_STRATEGY_VERLET : NW_STRATEGY_SORTED;
 }
 
 // Kernel parameter block for a configuration and step size.

@@ -144,10 +144,10 @@ __global__ void __launch_bounds__(256) scatter_kernel(const uint32_t* __restrict
     if (i < n) tmp[offset[hash[i]] + slot[i]] = i;
 }
 
-__global__ void __launch_bounds__(256) pair_ref_kernel(const DevParams P, const StepBuffers S)
+// collideFilamentsKernel's force on the bead at sorted position p, from the
+// sorted arrays in global memory (added to force[original index]).
+__device__ __forceinline__ void ref_pair_bead(const DevParams& P, const StepBuffers& S, uint32_t p)
 {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P.nb) return;
     const float3 r = f3(S.sorted_pos[p]);
     const float3 v = f3(S.sorted_vel[p]);
     const float3 t = f3(S.sorted_tan[p]);
@@ -187,6 +187,217 @@ __global__ void __launch_bounds__(256) pair_ref_kernel(const DevParams P, const 
     F.z += total.z;
     S.force[me] = F;
     if (!finite3(f3(F))) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
+}
+
+__global__ void __launch_bounds__(256) pair_ref_kernel(const DevParams P, const StepBuffers S)
+{
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < P.nb) ref_pair_bead(P, S, p);
+}
+
+// ---- REF_DEM pair pass, cell-tiled (single z layer) ---------------------------
+//
+// The thread-per-bead form above (the reference's own layout) spends most of
+// its issue slots on divergence: each lane walks 27 cells of 0-2 members and
+// branches per member (8 of 32 lanes active in the reference's kernel on the
+// 400k-bead lattice).  Here a block takes a tile of kRefTX x kRefTY cells of
+// the sorted order, stages the members of the tile and its one-cell halo
+// (pos, vel, tangent, original index and filament) in shared memory with
+// coalesced loads, and gives each central bead a group of kRefG lanes that
+// stride over its candidates: the members of the 3 x 3 halo cells around its
+// own, which lie in three contiguous runs of the staged arrays (one per halo
+// row, cells x-1 .. x+1).  The group's partial sums are combined by shuffles
+// in a fixed order, so results do not depend on scheduling.  With one z layer
+// every (x, y) neighbour cell is reached by the reference's three z offsets,
+// so the bead's sum is added three times; a cell reached by two x or y offsets
+// (grids narrower than 3 cells) appears twice in the halo and is summed twice,
+// as in the reference.  A tile whose halo holds more than kRefStage members
+// takes the thread-per-bead form.  Same pair laws as collideCell
+// (particles_kernel_impl.cuh:427-556), with the divisions by the separation
+// taken from a Newton-refined reciprocal.
+
+__device__ __forceinline__ float3 ref_pair_law(const DevParams& P, float3 r, float3 v, float3 t, float3 r2, float3 v2,
+                                               float3 t2, bool same, bool bonded)
+{
+    float3 rel = r2 - r;
+    min_image(P, rel);
+    const float q = dot3(rel, rel);
+    const float d = sqrt_nr(q, rsqrtf(q));
+    const float id = rcp_nr(d);
+    const float3 n = rel * id;
+    float3 F = zero3();
+    const float cd = P.radius + P.radius;
+    if (bonded) {
+        // bondHookean (:466-473)
+        F = (-P.bond_k * (P.bond_r0 - d)) * n;
+    } else if (d < cd) {
+        // collideParticles (:427-462)
+        const float3 rv = v2 - v;
+        const float3 tv = rv - dot3(rv, n) * n;
+        F = (-P.spring * (cd - d)) * n;
+        F += P.damping * rv;
+        F += P.shear * tv;
+    }
+    // extensileForce (:477-487): other filaments, anti-aligned tangents
+    if (!same && dot3(t, t2) < -0.5f) F += ((-P.activity) * (t - t2)) * (0.5f * id);
+    return F;
+}
+
+__global__ void __launch_bounds__(kRefThreads) pair_ref_tiled_kernel(const DevParams P, const StepBuffers S)
+{
+    extern __shared__ float4 smr[];
+    float4* spos = smr;
+    float4* svel = spos + kRefStage;
+    float4* stan = svel + kRefStage;
+    uint32_t* sidx = reinterpret_cast<uint32_t*>(stan + kRefStage);  // original index
+    uint32_t* sfil = sidx + kRefStage;                               // its filament
+    uint32_t* soff = sfil + kRefStage;                               // kRefHalo + 1 staged offsets
+    uint32_t* sbeg = soff + kRefHalo + 1;                            // sorted start of each halo cell
+    __shared__ uint32_t s_total, s_bad;
+    __shared__ uint32_t wsum[kRefThreads / 32];
+
+    const uint32_t tid = threadIdx.x;
+    const uint32_t tiles_x = (P.grid[0] + kRefTX - 1) / kRefTX;
+    const int x0 = (int)((blockIdx.x % tiles_x) * kRefTX);
+    const int y0 = (int)((blockIdx.x / tiles_x) * kRefTY);
+
+    // 1. member counts of the halo cells (halo row-major), exclusive scan
+    uint32_t cnt = 0, beg = 0;
+    if (tid < kRefHalo) {
+        const int hx = (int)(tid % kRefHX), hy = (int)(tid / kRefHX);
+        const uint32_t h = cell_hash(P, cell_coord(P, 0, x0 + hx - 1), cell_coord(P, 1, y0 + hy - 1), 0u);
+        uint32_t s1;
+        if (cell_range(P, S, h, beg, s1)) cnt = s1 - beg;
+    }
+    const uint32_t lane = tid & 31u, warp = tid >> 5;
+    const uint32_t inc = warp_incl_scan(cnt);
+    if (lane == 31u) wsum[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < kRefThreads / 32 ? wsum[lane] : 0u;
+        w = warp_incl_scan(w);
+        if (lane < kRefThreads / 32) wsum[lane] = w;
+    }
+    __syncthreads();
+    const uint32_t excl = inc - cnt + (warp ? wsum[warp - 1] : 0u);
+    if (tid < kRefHalo) {
+        soff[tid] = excl;
+        sbeg[tid] = beg;
+    }
+    if (tid == kRefThreads - 1) {
+        s_total = excl + cnt;
+        soff[kRefHalo] = excl + cnt;
+        s_bad = 0u;
+    }
+    __syncthreads();
+    const uint32_t total = s_total;
+    if (total > kRefStage) {
+        // crowded tile: the thread-per-bead form for its central cells
+        for (uint32_t hy = 1; hy <= kRefTY; ++hy) {
+            if (y0 + (int)hy - 1 >= (int)P.grid[1]) break;
+            for (uint32_t hx = 1 + warp; hx <= kRefTX; hx += kRefThreads / 32) {
+                if (x0 + (int)hx - 1 >= (int)P.grid[0]) break;
+                const uint32_t c = hy * kRefHX + hx;
+                const uint32_t n = soff[c + 1] - soff[c], b = sbeg[c];
+                for (uint32_t k = lane; k < n; k += 32u) ref_pair_bead(P, S, b + k);
+            }
+        }
+        return;
+    }
+    // 2. stage the members: element e of halo cell c is sorted position sbeg[c] + e - soff[c]
+    for (uint32_t e = tid; e < total; e += kRefThreads) {
+        uint32_t lo = 0, hi = kRefHalo;  // the last c with soff[c] <= e
+        while (hi - lo > 1u) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (soff[mid] <= e) lo = mid;
+            else hi = mid;
+        }
+        const uint32_t j = sbeg[lo] + (e - soff[lo]);
+        spos[e] = __ldg(&S.sorted_pos[j]);
+        svel[e] = __ldg(&S.sorted_vel[j]);
+        stan[e] = __ldg(&S.sorted_tan[j]);
+        const uint32_t o = __ldg(&S.sorted_index[j]);
+        if (o >= P.nb) s_bad = 1u;
+        sidx[e] = o;
+        sfil[e] = o / P.L;
+    }
+    __syncthreads();
+    if (s_bad) {
+        if (tid == 0) atomicOr(S.err, (uint32_t)NW_EFLAG_BAD_INDEX);
+        return;
+    }
+    // 3. central beads (cells of the tile inside the grid), kRefG lanes each
+    uint32_t row_lo[kRefTY], row_n[kRefTY], nc = 0;
+    const uint32_t nx = (uint32_t)max(0, min((int)kRefTX, (int)P.grid[0] - x0));
+#pragma unroll
+    for (uint32_t r = 0; r < kRefTY; ++r) {
+        const uint32_t hy = r + 1;
+        const uint32_t w = y0 + (int)hy - 1 < (int)P.grid[1] ? nx : 0u;
+        row_lo[r] = soff[hy * kRefHX + 1];
+        row_n[r] = soff[hy * kRefHX + 1 + w] - row_lo[r];
+        nc += row_n[r];
+    }
+    constexpr uint32_t kBeadsPerPass = kRefThreads / kRefG;
+    const uint32_t g = tid % kRefG;
+    const uint32_t passes = (nc + kBeadsPerPass - 1) / kBeadsPerPass;
+    for (uint32_t pass = 0; pass < passes; ++pass) {
+        const uint32_t c0 = pass * kBeadsPerPass + tid / kRefG;
+        const bool live = c0 < nc;
+        float3 sum = zero3();
+        uint32_t q = 0;
+        if (live) {
+            uint32_t hy = 1, c = c0;
+#pragma unroll
+            for (uint32_t r = 0; r < kRefTY; ++r) {
+                if (c < row_n[r]) {
+                    q = row_lo[r] + c;
+                    hy = r + 1;
+                    break;
+                }
+                c -= row_n[r];
+            }
+            // the bead's halo cell: the last cell of its row with soff <= q
+            uint32_t lo = hy * kRefHX + 1, hi = hy * kRefHX + kRefTX + 1;
+            while (hi - lo > 1u) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (soff[mid] <= q) lo = mid;
+                else hi = mid;
+            }
+            const uint32_t hx = lo - hy * kRefHX;
+            const float3 r = f3(spos[q]), v = f3(svel[q]), t = f3(stan[q]);
+            const uint32_t me = sidx[q], fI = sfil[q], cI = me - fI * P.L;
+            const uint32_t a0 = soff[(hy - 1) * kRefHX + hx - 1], n0 = soff[(hy - 1) * kRefHX + hx + 2] - a0;
+            const uint32_t a1 = soff[hy * kRefHX + hx - 1], n1 = soff[hy * kRefHX + hx + 2] - a1;
+            const uint32_t a2 = soff[(hy + 1) * kRefHX + hx - 1], n2 = soff[(hy + 1) * kRefHX + hx + 2] - a2;
+            const uint32_t m = n0 + n1 + n2;
+            for (uint32_t k = g; k < m; k += kRefG) {
+                const uint32_t j = k < n0 ? a0 + k : (k < n0 + n1 ? a1 + (k - n0) : a2 + (k - n0 - n1));
+                const uint32_t o = sidx[j];
+                if (o == me) continue;
+                const uint32_t fJ = sfil[j], cJ = o - fJ * P.L;
+                const bool same = fI == fJ;
+                const bool bonded = same && ((cI + 1u == cJ) || (cI - 1u == cJ));
+                sum += ref_pair_law(P, r, v, t, f3(spos[j]), f3(svel[j]), f3(stan[j]), same, bonded);
+            }
+        }
+        // fixed-order combination of the group's partial sums
+#pragma unroll
+        for (uint32_t o = 1; o < kRefG; o <<= 1) {
+            sum.x += __shfl_xor_sync(0xffffffffu, sum.x, o, kRefG);
+            sum.y += __shfl_xor_sync(0xffffffffu, sum.y, o, kRefG);
+            sum.z += __shfl_xor_sync(0xffffffffu, sum.z, o, kRefG);
+        }
+        if (live && g == 0) {
+            const uint32_t me = sidx[q];
+            const float3 tot = (sum + sum) + sum;  // the three z offsets of one layer
+            float4 F = S.force[me];
+            F.x += tot.x;
+            F.y += tot.y;
+            F.z += tot.z;
+            S.force[me] = F;
+            if (!finite3(f3(F))) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
+        }
+    }
 }
 
 __global__ void __launch_bounds__(256) pair_wca_kernel(const DevParams P, const StepBuffers S)

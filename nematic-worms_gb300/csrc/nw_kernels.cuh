@@ -446,6 +446,18 @@ __device__ __forceinline__ float3 ref_cell_sum(const DevParams& P, const StepBuf
 // z, y, x order, which reproduces the reference's accumulation exactly.
 __global__ void __launch_bounds__(256) pair_ref_kernel(const DevParams P, const StepBuffers S);
 
+// REF_DEM pair pass over tiles of kRefTX x kRefTY cells of a single z layer
+// (layout in nw_kernels.cu).  Grid: ceil(gx / kRefTX) * ceil(gy / kRefTY)
+// blocks of kRefThreads with kRefSmem bytes of dynamic shared memory (above
+// the default 48 KB: the kernel's attribute is raised when a system is made).
+constexpr uint32_t kRefTX = 32, kRefTY = 4, kRefG = 4, kRefThreads = 256;
+constexpr uint32_t kRefHX = kRefTX + 2, kRefHalo = kRefHX * (kRefTY + 2);
+constexpr uint32_t kRefStage = 1024;
+constexpr size_t kRefSmem = (size_t)kRefStage * (3 * 16 + 2 * 4) + (size_t)(2 * kRefHalo + 1) * 4;
+static_assert(kRefHalo <= kRefThreads, "one thread per halo cell");
+static_assert(32 % kRefG == 0, "lane groups within a warp");
+__global__ void __launch_bounds__(kRefThreads) pair_ref_tiled_kernel(const DevParams P, const StepBuffers S);
+
 // Neighbour cell c + o (o in -1..1) of an axis of G cells as the
 // distinct-cell visit takes it: wrapped on periodic axes, absent beyond a
 // wall, and absent when an earlier offset already gave the same cell

@@ -36,8 +36,12 @@ constexpr int kMaxDevices = 64;
 uint32_t* g_scratch_addr[kMaxDevices] = {};
 std::mutex g_setup_mu;
 
-// Device address of the scratch on the current device, looked up once per
-// device (the symbol's host-side name is not a device address).
+// Device address of the scratch on the current device (the symbol's
+// host-side name is not a device address).  Looked up again on every call
+// made outside stream capture, so that a context re-created after
+// cudaDeviceReset (which can place the symbol elsewhere) is picked up; calls
+// made while the legacy stream captures use the address of the last call
+// made outside capture on this device.
 nw_status scratch_address(uint32_t** out)
 {
     int dev = 0;
@@ -45,8 +49,18 @@ nw_status scratch_address(uint32_t** out)
         cudaGetLastError();
         return NW_ERR_CUDA;
     }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(0, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        return NW_ERR_CUDA;
+    }
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_addr[dev]) {
+    if (!g_scratch_addr[dev] || cap == cudaStreamCaptureStatusNone) {
+        if (cap != cudaStreamCaptureStatusNone) {
+            std::fprintf(stderr, "[nwgb] nw_sort_particles_noalloc: first call on a device made inside stream "
+                                 "capture; make it once outside capture first\n");
+            return NW_ERR_INVALID;
+        }
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_sort_scratch);
         if (e != cudaSuccess || !p) {
@@ -76,6 +90,14 @@ extern "C" int nw_sort_particles_noalloc(uint* dGridParticleHash, uint* dGridPar
     }
     if (numParticles < 2) return NW_OK;
     if (!dGridParticleHash || !dGridParticleIndex) return NW_ERR_INVALID;
+    // an error left by earlier, unrelated work is reported here and left in
+    // place for its owner, so that the check after the launches below only
+    // sees this call's own launches
+    if (cudaPeekAtLastError() != cudaSuccess) {
+        std::fprintf(stderr, "[nwgb] nw_sort_particles_noalloc: a CUDA error is pending from earlier work: %s\n",
+                     cudaGetErrorString(cudaPeekAtLastError()));
+        return NW_ERR_CUDA;
+    }
     if (radix_scratch_layout(kNoAllocMaxKeys, nullptr, nullptr) > kNoAllocWords) return NW_ERR_INVALID;
     uint32_t* base = nullptr;
     const nw_status st = scratch_address(&base);

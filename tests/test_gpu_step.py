@@ -69,6 +69,33 @@ def make_case(kind: str, lib):
         pos, vel, tan = reference_reset(cfg)
         rng = np.random.default_rng(4)
         pos[:cfg.n_beads, :2] += rng.normal(0, 0.05, (cfg.n_beads, 2)).astype(np.float32)
+    elif kind in ("ref_strip", "ref_alias"):
+        # REF_DEM grids narrower than the pair pass's 32 x 4 cell tiles: a
+        # 16 x 8 strip, and 2 x 16 where the x offsets -1 and +1 reach the
+        # same cell (the reference then visits it twice)
+        M, L, grid = (40, 4, (16, 8, 1)) if kind == "ref_strip" else (10, 2, (2, 16, 1))
+        cfg = abi.default_config(abi.NW_MODEL_REF_DEM, M, L, grid, False, lib)
+        cfg.bond_r0 = 0.8
+        cfg.bend_k = 10.0
+        cfg.activity = 0.5
+        cfg.spring = 57.0
+        cfg.kT = 0.1
+        cfg.gamma = 2.0
+        cfg.seed = 14
+        rng = np.random.default_rng(15)
+        pos = np.zeros((cfg.n_beads, 4), np.float32)
+        lo = np.array([cfg.origin[0], cfg.origin[1]])
+        hi = lo + np.array([cfg.box[0], cfg.box[1]])
+        for w in range(M):
+            head = rng.uniform(lo + 0.5, hi - 0.5 - np.array([0.0, 0.8 * (L - 1)]))
+            for k in range(L):
+                pos[w * L + k, :2] = head + np.array([rng.normal(0, 0.05), 0.8 * k])
+        pos[:, 3] = cfg.radius
+        vel = np.zeros_like(pos)
+        vel[:, :2] = rng.normal(0, 0.3, (cfg.n_beads, 2))
+        vel[:, 3] = cfg.mass
+        tan = np.zeros_like(pos)
+        tan[:, 1] = 1.0
     elif kind in ("wca_3d", "ref_3d"):
         # 3D grids: straight worms along x on a jittered y-z lattice of rows
         if kind == "wca_3d":
@@ -187,7 +214,8 @@ def check_step_parity(cfg, g, o, o64, pos0):
         assert e64 < fp64_bound(m(o, o64)), (k, "fp64", e64, m(o, o64))
 
 
-CASES = ["wca", "wca_srd", "wca_srd_dense", "wca_srd_rounds", "wca_srd_packed", "wca_reverse", "wca_3d", "ref", "ref_srd", "ref_walls", "ref_3d"]
+CASES = ["wca", "wca_srd", "wca_srd_dense", "wca_srd_rounds", "wca_srd_packed", "wca_reverse", "wca_3d", "ref", "ref_srd",
+         "ref_walls", "ref_3d", "ref_strip", "ref_alias"]
 STRATEGIES = [abi.NW_STRATEGY_CELL_LISTS, abi.NW_STRATEGY_SORTED, abi.NW_STRATEGY_VERLET]
 # launches of one update: (bead step, SRD collision) + the step counter; Verlet systems
 # add the on-demand cell-list kernel
