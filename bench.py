@@ -449,6 +449,17 @@ def ref_dem_r1(warmup, steps, stream):
             launches / steps}
 
 
+def dist_group(world):
+    """The NCCL process group of a multi-rank run (None for one rank)."""
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+
+    if not dist.is_initialized():
+        dist.init_process_group("nccl", init_method="env://")
+    return dist
+
+
 def run_reference_cuda(args):
     """The reference's own CUDA build (its kernels compiled for sm_103a from its
     source, launched as its C-ABI layer does, thrust sort and cuRAND) running
@@ -557,11 +568,13 @@ def run_ours(args):
     hv[:] = sysm.get_array(abi.NW_VELOCITY, 0, nb)
 
     def e2e_step():
-        sysm.set_array(abi.NW_POSITION, hp, 0)
-        sysm.set_array(abi.NW_VELOCITY, hv, 0)
+        # inputs from and results to pinned host memory, one synchronisation
+        sysm.set_array_async(abi.NW_POSITION, hp, 0)
+        sysm.set_array_async(abi.NW_VELOCITY, hv, 0)
         sysm.step(1, cfg.dt)
-        sysm.get_array(abi.NW_POSITION, 0, nb, out=hp)
-        sysm.get_array(abi.NW_VELOCITY, 0, nb, out=hv)
+        sysm.get_array_async(abi.NW_POSITION, hp, 0)
+        sysm.get_array_async(abi.NW_VELOCITY, hv, 0)
+        sysm.sync()
 
     for _ in range(GAP):  # one single-step graph per collision phase, built before the clock starts
         e2e_step()
@@ -611,7 +624,8 @@ def run_ours(args):
                            "note": "each repeat restarts from the checkpoint taken after the warm-up"},
                 "e2e": {"value": e2e_value, "unit": "bead-steps/s", "h2d_bytes_per_step": nb * 32,
                         "d2h_bytes_per_step": nb * 32, "steps": e2e_steps,
-                        "path": "nw_set_array(pos, vel) + nw_step(1) + nw_get_array(pos, vel) per step, pinned host"},
+                        "path": "nw_set_array_async(pos, vel) + nw_step(1) + nw_get_array_async(pos, vel) + "
+                                "nw_sync per step, pinned host; the host link measures ~200 GB/s per direction"},
                 "gpu_launches": gpu_launches, "roofline": roofline}
         if world == 1 and not args.no_extras:
             k_sub = min(args.steps, 1000)
@@ -656,9 +670,16 @@ def batch_block(args, steps=None):
 
     rank, world, local = env_rank()
     torch.cuda.set_device(local)
+    dist = dist_group(world)
     R = WORKLOADS["batch_256"]["batch"]
-    cfgs = batch_configs(R, seed=1000 * rank)
+    cfgs = batch_configs(R, seed=1000)
     states = [initial_state(c, seed=r, layout="rows") for r, c in enumerate(cfgs)]
+    if world > 1:
+        # one job of R replicas spread over the ranks by bead count
+        from nwgb.replicas import partition
+
+        mine = partition([c.n_beads for c in cfgs], world)[rank]
+        cfgs, states = [cfgs[r] for r in mine], [states[r] for r in mine]
     total = sum(c.n_beads for c in cfgs)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
@@ -693,8 +714,17 @@ def batch_block(args, steps=None):
     clk = clocks.stop()
     b.sync()
     launches = b.last_launch_count * nchunks
-    value = total * chunk * nchunks / (ms / 1e3)
+    value, ms = job_rate(dist, ms, total * chunk * nchunks, device="cuda")
     b.close()
+    if world > 1:
+        line = {"metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": world,
+                "steps": chunk * nchunks, "warmup": warm, "ms_per_step": ms / (chunk * nchunks),
+                "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "clocks": clk, "gpu_launches": launches,
+                "config": {"workload": "batch_256", "replicas": R, "parallelism": f"replicas bin-packed x{world}",
+                           "replicas_rank0": len(cfgs), "beads_rank0": total}}
+        dist.destroy_process_group()
+        return line
 
     # sequential: the same replicas one by one through the single-system step
     seq_steps = chunk
@@ -763,24 +793,34 @@ def adjoint_block(args):
     from nwgb.init import baseline_config, initial_state
     from nwgb.observables import PairSample, loss_s_cv, velocity_correlation
 
+    from nwgb.replicas import contiguous_block, loss_and_gradient_mean, replica_mean
+
     rank, world, local = env_rank()
     torch.cuda.set_device(local)
-    R = WORKLOADS["adjoint_64x4k"]["adjoint"]
+    dist = dist_group(world)
+    R_all = WORKLOADS["adjoint_64x4k"]["adjoint"]
     H, SEG = 200, 20
-    cfg = baseline_config(0, seed=7)
-    states = [initial_state(cfg, seed=r, layout="patches") for r in range(R)]
+    # this rank's replicas: an equal contiguous block, so that replica r keeps
+    # its seed (7 + r), initial state and pair sample on any rank
+    mine = contiguous_block(R_all, world, rank)
+    R = len(mine)
+    cfg = baseline_config(0, seed=7 + mine.start)
+    states = [initial_state(cfg, seed=r, layout="patches") for r in mine]
     pos = torch.from_numpy(np.concatenate([s[0] for s in states])).cuda()
     vel = torch.from_numpy(np.concatenate([s[1] for s in states])).cuda()
     ro = Rollout(cfg, R, H, SEG, 32)
     ro.set_state(pos, vel)
     box = [cfg.box[0], cfg.box[1], cfg.box[2]]
-    pairs = PairSample(R, cfg.n_beads, 20000, seed=1, device="cuda")
-    # C_target from a seeded run at the reference parameters
+    every = PairSample(R_all, cfg.n_beads, 20000, seed=1, device="cuda")
+    pairs = PairSample(1, cfg.n_beads, 1, seed=0, device="cuda")
+    pairs.i, pairs.j = every.i[mine.start:mine.stop], every.j[mine.start:mine.stop]
+    # C_target from a seeded run at the reference parameters (mean over all replicas)
     with torch.no_grad():
         p, v = ro.forward([1.0, 10.0, 57.0, 0.5])
-        target = velocity_correlation(p[:, :3].reshape(R, -1, 3).double(), v[:, :3].reshape(R, -1, 3).double(),
-                                      pairs, box).mean(0, keepdim=True)
-    fwd, bwd = [], []
+        cv = velocity_correlation(p[:, :3].reshape(R, -1, 3).double(), v[:, :3].reshape(R, -1, 3).double(), pairs,
+                                  box)
+        target = replica_mean(cv.sum(0), R, dist)[None, :]
+    fwd, bwd, red = [], [], []
     reps = max(3, min(10, args.steps // H))
     for k in range(args.warmup + reps):
         th = torch.tensor([1.1, 8.0, 50.0, 0.8], dtype=torch.float64, requires_grad=True)
@@ -788,12 +828,27 @@ def adjoint_block(args):
         L = loss_s_cv(p[:, :3].reshape(R, -1, 3).double(), v[:, :3].reshape(R, -1, 3).double(), cfg.filament_size,
                       box, pairs, target)
         L.backward()
+        t0 = time.perf_counter()
+        loss, grad = loss_and_gradient_mean(L, th.grad, R, dist)  # one all-reduce of 6 numbers
+        t_red = time.perf_counter() - t0
         f_ms, b_ms = ro.timings()
         if k >= args.warmup:
             fwd.append(f_ms)
             bwd.append(b_ms)
+            red.append(1e3 * t_red)
     f_ms, b_ms = statistics.median(fwd), statistics.median(bwd)
     ro.close()
+    if world > 1:
+        job, step_ms = job_rate(dist, f_ms + b_ms + statistics.median(red), R * cfg.n_beads * H, device="cuda")
+        line = {"metric": "bead-steps/s", "value": job, "unit": "bead-steps/s", "n_gpus": world, "steps": H * len(fwd),
+                "warmup": args.warmup, "ms_per_step": step_ms / H, "higher_is_better": True, "scaling": "strong",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "adjoint_64x4k", "replicas": R_all, "parallelism": f"replica blocks x{world}",
+                           "horizon": H, "segment": SEG},
+                "adjoint": {"forward_ms": f_ms, "backward_ms": b_ms, "allreduce_ms": statistics.median(red),
+                            "loss": float(loss), "grad": [float(x) for x in grad]}}
+        dist.destroy_process_group()
+        return line
     # production step on the same replicas (batched engine, one launch per step)
     cfgs = [baseline_config(0, seed=7 + r) for r in range(R)]
     stream = torch.cuda.Stream()

@@ -252,6 +252,15 @@ nw_status nw_get_counts(const nw_system* sys, uint32_t* n_beads, uint32_t* n_sol
 nw_status nw_set_array(nw_system* sys, int array, const void* host, uint32_t start, uint32_t count);
 /* Replaces: ParticleSystem::getArray (simulation/particleSystem.cpp:534-559). */
 nw_status nw_get_array(nw_system* sys, int array, void* host, uint32_t start, uint32_t count);
+/* nw_set_array / nw_get_array enqueued on the system's stream without waiting
+ * (no counterpart in the reference, whose copies are synchronous): the host
+ * buffer must stay untouched until nw_sync returns, and is best pinned, so
+ * that the copies of a step (inputs, nw_step, results) run back to back on the
+ * device with one synchronisation.  Arrays computed when read (sorted order,
+ * cell bounds, reference hashes, tangents of lazy systems) are produced on the
+ * stream as well. */
+nw_status nw_set_array_async(nw_system* sys, int array, const void* host, uint32_t start, uint32_t count);
+nw_status nw_get_array_async(nw_system* sys, int array, void* host, uint32_t start, uint32_t count);
 /* Device pointer of an array (zero-copy access; valid until nw_destroy).  The
  * double-buffered state of the cell-list / Verlet paths moves between two
  * buffers with the step parity: ask again after stepping.  NW_POSITION marks

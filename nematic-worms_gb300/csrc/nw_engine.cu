@@ -446,7 +446,7 @@ enum class Dir { ToDevice, ToHost };
 
 // Copy `count` elements of an API array between host and device.  Position /
 // velocity arrays are beads [0, nb) then solvent [nb, nb + ns) in two stores.
-nw_status transfer(nw_system* s, int array, void* host, uint32_t start, uint32_t count, Dir dir)
+nw_status transfer(nw_system* s, int array, void* host, uint32_t start, uint32_t count, Dir dir, bool wait = true)
 {
     const uint32_t cur = cur_buffer(s);
     const StepBuffers& B = s->B;
@@ -531,7 +531,7 @@ nw_status transfer(nw_system* s, int array, void* host, uint32_t start, uint32_t
         e = dir == Dir::ToDevice ? cudaMemcpyAsync(d, h, (b - a) * elem, cudaMemcpyHostToDevice, s->stream)
                                  : cudaMemcpyAsync(h, d, (b - a) * elem, cudaMemcpyDeviceToHost, s->stream);
     }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess && wait) e = cudaStreamSynchronize(s->stream);
     if (dir == Dir::ToDevice) {
         s->sorted_for = ~0ull;
         s->hash_for = ~0ull;
@@ -775,6 +775,18 @@ nw_status nw_get_array(nw_system* s, int array, void* host, uint32_t start, uint
 {
     if (!s || (!host && count)) return NW_ERR_INVALID;
     return transfer(s, array, host, start, count, Dir::ToHost);
+}
+
+nw_status nw_set_array_async(nw_system* s, int array, const void* host, uint32_t start, uint32_t count)
+{
+    if (!s || (!host && count)) return NW_ERR_INVALID;
+    return transfer(s, array, const_cast<void*>(host), start, count, Dir::ToDevice, false);
+}
+
+nw_status nw_get_array_async(nw_system* s, int array, void* host, uint32_t start, uint32_t count)
+{
+    if (!s || (!host && count)) return NW_ERR_INVALID;
+    return transfer(s, array, host, start, count, Dir::ToHost, false);
 }
 
 nw_status nw_device_array(nw_system* s, int array, void** dptr)

@@ -198,6 +198,8 @@ HANDLE_API = [
     ("nw_get_counts", C.c_int, [_sysp, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
     ("nw_set_array", C.c_int, [_sysp, C.c_int, _P, _u32, _u32]),
     ("nw_get_array", C.c_int, [_sysp, C.c_int, _P, _u32, _u32]),
+    ("nw_set_array_async", C.c_int, [_sysp, C.c_int, _P, _u32, _u32]),
+    ("nw_get_array_async", C.c_int, [_sysp, C.c_int, _P, _u32, _u32]),
     ("nw_device_array", C.c_int, [_sysp, C.c_int, C.POINTER(_P)]),
     ("nw_zero_forces", C.c_int, [_sysp]),
     ("nw_step", C.c_int, [_sysp, C.c_int, _f32]),

@@ -98,6 +98,23 @@ class System:
         check(self.lib.nw_get_array(self._h, which, out.ctypes.data, start, count), "nw_get_array")
         return out
 
+    def set_array_async(self, which: int, data: np.ndarray, start: int = 0) -> None:
+        """nw_set_array_async: enqueue the copy of `data` (kept alive and
+        unchanged by the caller until sync(); best pinned) on the stream."""
+        want = np.float32 if which in _FLOAT4 else np.uint32
+        if data.dtype != want or not data.flags["C_CONTIGUOUS"]:
+            raise ValueError("data must be a C-contiguous array of the array's element type")
+        n = data.shape[0]
+        check(self.lib.nw_set_array_async(self._h, which, data.ctypes.data, start, n), "nw_set_array_async")
+
+    def get_array_async(self, which: int, out: np.ndarray, start: int = 0) -> None:
+        """nw_get_array_async: enqueue the copy into `out` (valid after sync())."""
+        want = np.float32 if which in _FLOAT4 else np.uint32
+        if out.dtype != want or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a C-contiguous array of the array's element type")
+        check(self.lib.nw_get_array_async(self._h, which, out.ctypes.data, start, out.shape[0]),
+              "nw_get_array_async")
+
     def device_ptr(self, which: int) -> int:
         p = C.c_void_p()
         check(self.lib.nw_device_array(self._h, which, C.byref(p)), "nw_device_array")
