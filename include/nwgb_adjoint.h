@@ -38,6 +38,9 @@ typedef struct nw_adjoint nw_adjoint;
 nw_status nw_adj_create(const NwConfig* cfg, int n_replicas, int horizon, int segment, int precision,
                         nw_adjoint** out);
 nw_status nw_adj_destroy(nw_adjoint* a);
+/* Stream of the rollout's work; NULL selects the handle's own stream, which
+ * is ordered with the legacy default stream (work queued there before a call
+ * is finished before the rollout reads its inputs). */
 nw_status nw_adj_set_stream(nw_adjoint* a, void* stream);
 
 /* Initial positions and velocities (device float4 arrays); forces start at 0. */
@@ -46,6 +49,12 @@ nw_status nw_adj_set_state(nw_adjoint* a, const float* d_pos, const float* d_vel
 /* Run `horizon` steps with theta = {eps, k_bend, k_bond, F_act}; writes the
  * final positions and velocities to device float4 arrays.  Synchronous. */
 nw_status nw_adj_forward(nw_adjoint* a, const double theta[4], float* d_pos_out, float* d_vel_out);
+
+/* The final state of the last forward as (x, y, z, 0) double quadruples
+ * (device arrays of n_replicas * n_beads * 4 doubles; either may be NULL),
+ * unrounded at precision 64: what finite differences of the FP64 forward
+ * need, where float4 outputs would round the loss.  Synchronous. */
+nw_status nw_adj_final_state_f64(nw_adjoint* a, double* d_pos_out, double* d_vel_out);
 
 /* Given dL/d(final positions) and dL/d(final velocities) (device float4
  * arrays, w ignored), write dL/dtheta of the last forward.  Synchronous. */

@@ -537,6 +537,20 @@ __global__ void to_f4_kernel(const typename Vec4<T>::type* __restrict__ a, float
     }
 }
 
+// xyz of the state in double (x, y, z, 0) quadruples, at either precision
+template <class T>
+__global__ void to_d4_kernel(const typename Vec4<T>::type* __restrict__ a, double* __restrict__ b, uint32_t n)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const V3<T> x = ld3<T>(a, i);
+        b[4 * (size_t)i] = (double)x.x;
+        b[4 * (size_t)i + 1] = (double)x.y;
+        b[4 * (size_t)i + 2] = (double)x.z;
+        b[4 * (size_t)i + 3] = 0.0;
+    }
+}
+
 uint32_t nblocks(uint32_t n) { return (n + 255u) / 256u; }
 
 }  // namespace
@@ -814,7 +828,10 @@ nw_status nw_adj_create(const NwConfig* cfg, int n_replicas, int horizon, int se
     }
     a->ncap = cfg->neighbor_capacity ? cfg->neighbor_capacity : 32u;
     a->cap = 16;
-    if (cudaStreamCreateWithFlags(&a->own, cudaStreamNonBlocking) != cudaSuccess) {
+    // a blocking stream: the rollout's own work is ordered with the legacy
+    // default stream, on which callers such as torch produce the upstream
+    // gradients it reads (a non-blocking stream could read them unfinished)
+    if (cudaStreamCreateWithFlags(&a->own, cudaStreamDefault) != cudaSuccess) {
         delete a;
         return NW_ERR_CUDA;
     }
@@ -903,6 +920,24 @@ nw_status nw_adj_forward(nw_adjoint* a, const double theta[4], float* d_pos_out,
         if (!std::isfinite(theta[q])) return NW_ERR_INVALID;
     return a->prec == 64 ? forward_t<double>(a, theta, d_pos_out, d_vel_out)
                          : forward_t<float>(a, theta, d_pos_out, d_vel_out);
+}
+
+nw_status nw_adj_final_state_f64(nw_adjoint* a, double* d_pos_out, double* d_vel_out)
+{
+    if (!a || !a->have_forward) return NW_ERR_INVALID;
+    cudaError_t e = cudaSuccess;
+    if (a->prec == 64) {
+        using V = typename Vec4<double>::type;
+        if (d_pos_out) to_d4_kernel<double><<<nblocks(a->N), 256, 0, a->stream>>>(static_cast<const V*>(a->r), d_pos_out, a->N);
+        if (d_vel_out) to_d4_kernel<double><<<nblocks(a->N), 256, 0, a->stream>>>(static_cast<const V*>(a->v), d_vel_out, a->N);
+    } else {
+        using V = typename Vec4<float>::type;
+        if (d_pos_out) to_d4_kernel<float><<<nblocks(a->N), 256, 0, a->stream>>>(static_cast<const V*>(a->r), d_pos_out, a->N);
+        if (d_vel_out) to_d4_kernel<float><<<nblocks(a->N), 256, 0, a->stream>>>(static_cast<const V*>(a->v), d_vel_out, a->N);
+    }
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(a->stream);
+    return e == cudaSuccess ? NW_OK : st_of(e);
 }
 
 nw_status nw_adj_backward(nw_adjoint* a, const float* d_grad_pos, const float* d_grad_vel, double grad_theta[4])

@@ -300,6 +300,7 @@ ADJOINT_API = [
     ("nw_adj_set_state", C.c_int, [_ap, _P, _P]),
     ("nw_adj_forward", C.c_int, [_ap, C.POINTER(C.c_double), _P, _P]),
     ("nw_adj_backward", C.c_int, [_ap, _P, _P, C.POINTER(C.c_double)]),
+    ("nw_adj_final_state_f64", C.c_int, [_ap, _P, _P]),
     ("nw_adj_timings", C.c_int, [_ap, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
 ]
 

@@ -66,6 +66,16 @@ class Rollout:
               "nw_adj_forward")
         return pos, vel
 
+    def final_state_f64(self) -> tuple[torch.Tensor, torch.Tensor]:
+        """Final (positions, velocities) of the last forward, (n, 4) float64
+        CUDA tensors (w = 0), unrounded at precision 64."""
+        pos = torch.empty((self.n, 4), dtype=torch.float64, device="cuda")
+        vel = torch.empty((self.n, 4), dtype=torch.float64, device="cuda")
+        self._stream()
+        check(self.lib.nw_adj_final_state_f64(self.h, C.c_void_p(pos.data_ptr()), C.c_void_p(vel.data_ptr())),
+              "nw_adj_final_state_f64")
+        return pos, vel
+
     def backward(self, grad_pos: torch.Tensor, grad_vel: torch.Tensor) -> np.ndarray:
         gp = grad_pos.detach().to(device="cuda", dtype=torch.float32).contiguous()
         gv = grad_vel.detach().to(device="cuda", dtype=torch.float32).contiguous()

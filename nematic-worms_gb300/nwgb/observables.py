@@ -12,8 +12,8 @@ order from the 3D Q tensor Q = 1.5 <t t> - I/2
 (analysis/analyze_correlations.py:22-28), whose largest eigenvalue for
 planar tangents is 1/4 + 3/4 S2 with S2 = |<exp(2 i theta)>|; the loss uses
 S2.  The velocity correlation C_v(r) (mean v_i . v_j of sampled bead pairs
-at distance r, normalised by <|v|^2>) has no reference definition and is
-defined here.
+at distance r, normalised by <|v|^2>, with smooth bin weights) has no
+reference definition and is defined here.
 """
 from __future__ import annotations
 
@@ -79,24 +79,42 @@ class PairSample:
         self.i, self.j = i.to(device), j.to(device)
 
 
+def bin_weights(d: torch.Tensor, r_max: float, bins: int) -> torch.Tensor:
+    """Weights (..., bins) of distances d on `bins` bins of width r_max / bins
+    by the quadratic B-spline around the bin centres: each distance spreads
+    over its nearest centre and the two beside it with weights summing to 1
+    (weight beyond the first or last bin is dropped).  The weights, and
+    every average built from them, are continuously differentiable in d, so
+    the loss below has the gradient its adjoint computes; hard bin membership
+    would make it jump wherever a pair crosses a bin edge."""
+    x = d / (r_max / bins) - 0.5
+    c = torch.floor(x + 0.5)
+    t = x - c
+    w = torch.stack([0.5 * (0.5 - t) ** 2, 0.75 - t * t, 0.5 * (0.5 + t) ** 2], dim=-1)
+    idx = c.long()[..., None] + torch.tensor([-1, 0, 1], device=d.device)
+    ok = (idx >= 0) & (idx < bins)
+    out = torch.zeros(d.shape + (bins + 1,), dtype=d.dtype, device=d.device)
+    out.scatter_add_(-1, torch.where(ok, idx, torch.full_like(idx, bins)), torch.where(ok, w, torch.zeros_like(w)))
+    return out[..., :bins]
+
+
 def velocity_correlation(pos: torch.Tensor, vel: torch.Tensor, pairs: PairSample, box, r_max: float = 8.0,
                          bins: int = 32) -> torch.Tensor:
-    """C_v per replica and distance bin (R, bins): mean v_i . v_j over the
-    sampled pairs whose (minimum-image) distance falls in the bin, divided by
-    <|v|^2>.  Bin membership is taken from the positions without gradient."""
+    """C_v per replica and distance bin (R, bins): the mean of v_i . v_j over
+    the sampled pairs, each weighted into the bins of its (minimum-image)
+    distance by bin_weights, divided by <|v|^2>.  A bin's mean is its weighted
+    sum over its weight sum plus 1e-3 (so that nearly empty bins stay finite
+    and smooth)."""
     box = torch.as_tensor(box, dtype=pos.dtype, device=pos.device)
     ri = torch.gather(pos, 1, pairs.i[..., None].expand(-1, -1, 3))
     rj = torch.gather(pos, 1, pairs.j[..., None].expand(-1, -1, 3))
     vi = torch.gather(vel, 1, pairs.i[..., None].expand(-1, -1, 3))
     vj = torch.gather(vel, 1, pairs.j[..., None].expand(-1, -1, 3))
-    with torch.no_grad():
-        d = torch.linalg.norm(min_image(rj - ri, box), dim=-1)
-        k = torch.clamp((d / r_max * bins).long(), max=bins)  # bin `bins` = beyond r_max
-        onehot = torch.nn.functional.one_hot(k, bins + 1)[..., :bins].to(pos.dtype)
-        count = onehot.sum(dim=1).clamp(min=1.0)
+    d = torch.linalg.norm(min_image(rj - ri, box), dim=-1)
+    w = bin_weights(d, r_max, bins)
     dots = (vi * vj).sum(-1)
     v2 = (vel ** 2).sum(-1).mean(dim=1, keepdim=True)
-    return torch.einsum("rp,rpb->rb", dots, onehot) / count / v2
+    return torch.einsum("rp,rpb->rb", dots, w) / (w.sum(dim=1) + 1e-3) / v2
 
 
 def loss_s_cv(pos: torch.Tensor, vel: torch.Tensor, L: int, box, pairs: PairSample, cv_target: torch.Tensor,
