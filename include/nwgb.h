@@ -390,6 +390,53 @@ nw_status nw_find_defects(nw_system* sys, float cell_size, uint32_t flags, NwDef
 nw_status nw_sample_defects(nw_system* sys, const uint32_t* beads, int n_points, float radius, uint32_t flags,
                             int32_t* winding);
 
+/* ---- observables ----------------------------------------------------------- */
+
+/* Order parameters and temperatures of the current state (no counterpart in
+ * the reference's step; its offline analysis defines them,
+ * analysis/analyze_correlations.py:13-38 and analysis/afa/utils.py:35-49):
+ *  - bead tangents as in nw_find_defects (raw differences unless
+ *    NW_OBS_MIN_IMAGE; none for the first and last bead of the system);
+ *  - s_q3: the largest eigenvalue of Q = 1.5 <t t> - I / 2, the mean over all
+ *    beads (a bead without a tangent counts as t = 0), the reference's S;
+ *  - s_2d: |<exp(2 i a)>| over the beads with a tangent, a the angle of the
+ *    tangent's xy part; polar: |<t>| over all beads;
+ *  - bead_temperature <m |v|^2> / dim over beads, solvent_temperature over
+ *    the solvent;
+ *  - msd (NW_OBS_MSD): <|r - r_ref|^2> of unwrapped bead positions since
+ *    nw_observe_reset, unwrapped by the periodic images each bead crossed
+ *    between calls (call at least once per half box of motion; bead indices
+ *    must not move, so no filament reversal in between).
+ * Fixed-order double sums.  Synchronous. */
+#define NW_OBS_MIN_IMAGE 1u
+#define NW_OBS_MSD 2u
+typedef struct NwObservables {
+    double s_q3, s_2d, polar;
+    double bead_temperature, solvent_temperature;
+    double msd;
+    uint32_t n_beads, n_tangents, n_solvent, reserved;
+} NwObservables;
+nw_status nw_observe(nw_system* sys, uint32_t flags, NwObservables* out);
+/* Reference positions of the mean-square displacement := the current ones. */
+nw_status nw_observe_reset(nw_system* sys);
+/* Velocity correlation by distance of the sampled bead pairs (d_i[k], d_j[k])
+ * (device arrays of n_pairs indices): each pair's v_i . v_j enters the `bins`
+ * bins of width r_max / bins by the quadratic B-spline weights of its
+ * minimum-image distance (bins around its nearest bin centre, weights summing
+ * to 1; the weights nwgb.observables uses), sum_dot[b] = sum w v_i . v_j,
+ * sum_weight[b] = sum w (host arrays of `bins`, at most 128).  C_v(b) =
+ * sum_dot / (sum_weight + 1e-3) / <|v|^2>.  Fixed-order sums.  Synchronous. */
+nw_status nw_velocity_correlation(nw_system* sys, const uint32_t* d_i, const uint32_t* d_j, uint32_t n_pairs,
+                                  float r_max, uint32_t bins, double* sum_dot, double* sum_weight);
+/* Histogram of SRD cell temperatures sum m |v - u|^2 / (dim (n - 1)) (u the
+ * cell's mass-weighted mean velocity) over the cells of two or more members
+ * (beads and solvent) on the SRD grid shifted by `shift` (NULL: none):
+ * counts[b] for T in [b, b + 1) t_max / bins, counts[bins] above t_max,
+ * counts[bins + 1] the cells counted (host array of bins + 2).  Cell sums are
+ * 2^32 fixed-point integers (independent of thread order).  Synchronous. */
+nw_status nw_srd_temperature_histogram(nw_system* sys, const float shift[3], float t_max, uint32_t bins,
+                                       uint32_t* counts);
+
 /* Numerics self-check of the refined reciprocal, square root and quotient
  * the force laws use (no reference counterpart).  For host arrays a[n] and
  * b[n] of positive normal floats it writes, per element, out[4*i + 0..3] =

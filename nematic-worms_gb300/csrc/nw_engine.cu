@@ -279,6 +279,12 @@ void free_all(nw_system* s)
     s->defect_fixed = s->defect_acc = nullptr;
     s->defect_host = nullptr;
     s->defect_acc_bytes = 0;
+    cudaFree(s->obs_ws);
+    cudaFree(s->obs_msd);
+    cudaFree(s->obs_srd);
+    s->obs_ws = s->obs_msd = s->obs_srd = nullptr;
+    s->obs_ws_bytes = s->obs_msd_bytes = s->obs_srd_bytes = 0;
+    s->obs_msd_on = false;
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     s->own_stream = nullptr;
 }

@@ -43,4 +43,14 @@ struct nw_system {
     void* defect_acc = nullptr;
     size_t defect_acc_bytes = 0;
     uint32_t* defect_host = nullptr;
+    // observables workspace (nw_observables.cu): partial sums, the
+    // mean-square displacement's reference / last positions and images, the
+    // SRD cell sums; grown on demand
+    void* obs_ws = nullptr;
+    size_t obs_ws_bytes = 0;
+    void* obs_msd = nullptr;
+    size_t obs_msd_bytes = 0;
+    bool obs_msd_on = false;
+    void* obs_srd = nullptr;
+    size_t obs_srd_bytes = 0;
 };

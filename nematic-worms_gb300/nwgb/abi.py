@@ -180,6 +180,17 @@ class NwDefect(C.Structure):
     _fields_ = [("x", C.c_double), ("y", C.c_double), ("charge", C.c_float), ("cells", _u32)]
 
 
+class NwObservables(C.Structure):
+    """include/nwgb.h NwObservables."""
+
+    _fields_ = [("s_q3", C.c_double), ("s_2d", C.c_double), ("polar", C.c_double),
+                ("bead_temperature", C.c_double), ("solvent_temperature", C.c_double), ("msd", C.c_double),
+                ("n_beads", _u32), ("n_tangents", _u32), ("n_solvent", _u32), ("reserved", _u32)]
+
+
+NW_OBS_MIN_IMAGE = 1
+NW_OBS_MSD = 2
+
 # numpy view of an NwDefect array (same 24-byte layout)
 DEFECT_DTYPE = np.dtype([("x", "<f8"), ("y", "<f8"), ("charge", "<f4"), ("cells", "<u4")])
 
@@ -227,6 +238,10 @@ HANDLE_API = [
     ("nw_writer_close", C.c_int, [_P]),
     ("nw_find_defects", C.c_int, [_sysp, _f32, _u32, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     ("nw_sample_defects", C.c_int, [_sysp, C.c_void_p, C.c_int, _f32, _u32, C.c_void_p]),
+    ("nw_observe", C.c_int, [_sysp, _u32, C.POINTER(NwObservables)]),
+    ("nw_observe_reset", C.c_int, [_sysp]),
+    ("nw_velocity_correlation", C.c_int, [_sysp, _P, _P, _u32, _f32, _u32, _P, _P]),
+    ("nw_srd_temperature_histogram", C.c_int, [_sysp, _P, _f32, _u32, _P]),
 ]
 
 _fp = C.c_void_p  # device pointers are passed as integers

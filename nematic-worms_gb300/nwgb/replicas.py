@@ -65,7 +65,8 @@ def loss_and_gradient_mean(local_loss_mean: torch.Tensor, local_grad_mean: torch
     rank's mean over its own replicas (what nwgb.observables.loss_s_cv and the
     rollout's backward give): the rank's means are weighted by its replica
     count.  Returns (loss, grad) float64 tensors on every rank."""
-    s = torch.cat([local_grad_mean.detach().to(torch.float64).reshape(-1),
+    dev = local_loss_mean.device  # the loss's device (CUDA under NCCL, the CPU under gloo)
+    s = torch.cat([local_grad_mean.detach().to(device=dev, dtype=torch.float64).reshape(-1),
                    local_loss_mean.detach().to(torch.float64).reshape(1)]) * float(local_count)
     m = replica_mean(s, local_count, dist)
     return m[-1], m[:-1]

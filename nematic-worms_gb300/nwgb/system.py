@@ -174,6 +174,41 @@ class System:
         check(self.lib.nw_profile_steps(self._h, int(n), float(dt), buf, 32, C.byref(cnt)), "nw_profile_steps")
         return {buf[k].name.decode(): (buf[k].total_ms, int(buf[k].launches)) for k in range(cnt.value)}
 
+    # -- observables (computed on the device) -----------------------------------------------
+    def observe(self, min_image: bool = False, msd: bool = False) -> dict:
+        """Order parameters, temperatures and (after observe_reset) the mean-
+        square displacement of the current state (nw_observe)."""
+        o = abi.NwObservables()
+        flags = (abi.NW_OBS_MIN_IMAGE if min_image else 0) | (abi.NW_OBS_MSD if msd else 0)
+        check(self.lib.nw_observe(self._h, flags, C.byref(o)), "nw_observe")
+        return {f: getattr(o, f) for f, _ in o._fields_ if f != "reserved"}
+
+    def observe_reset(self) -> None:
+        check(self.lib.nw_observe_reset(self._h), "nw_observe_reset")
+
+    def velocity_correlation(self, i: np.ndarray, j: np.ndarray, r_max: float = 8.0, bins: int = 32):
+        """(sum of weighted v_i . v_j, sum of weights) per distance bin of the
+        sampled bead pairs (i[k], j[k]) (nw_velocity_correlation)."""
+        import torch
+
+        di = torch.from_numpy(np.ascontiguousarray(np.asarray(i, dtype=np.uint32)).view(np.int32)).cuda()
+        dj = torch.from_numpy(np.ascontiguousarray(np.asarray(j, dtype=np.uint32)).view(np.int32)).cuda()
+        sd = np.zeros(bins, np.float64)
+        sw = np.zeros(bins, np.float64)
+        torch.cuda.synchronize()
+        check(self.lib.nw_velocity_correlation(self._h, di.data_ptr(), dj.data_ptr(), di.numel(), float(r_max), bins,
+                                               sd.ctypes.data, sw.ctypes.data), "nw_velocity_correlation")
+        return sd, sw
+
+    def srd_temperature_histogram(self, t_max: float, bins: int = 64, shift=(0.0, 0.0, 0.0)) -> np.ndarray:
+        """Counts of SRD cells by temperature: bins of t_max / bins, then the
+        cells above t_max, then the cells counted (nw_srd_temperature_histogram)."""
+        out = np.zeros(bins + 2, np.uint32)
+        sh = (C.c_float * 3)(*[float(x) for x in shift])
+        check(self.lib.nw_srd_temperature_histogram(self._h, sh, float(t_max), bins, out.ctypes.data),
+              "nw_srd_temperature_histogram")
+        return out
+
     def find_defects(self, cell_size: float = 2.0, min_image: bool = False, max_defects: int = 4096) -> np.ndarray:
         """+1/2 and -1/2 defects of the director field of the current beads
         (analysis/find_defects.py:170-207 on the director field of
