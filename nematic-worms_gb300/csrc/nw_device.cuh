@@ -56,6 +56,7 @@ struct DevParams {
     float vl_r2;         // (lj_rcut + skin)^2
     float vl_half_skin;  // lists stay valid while the displacement bound is below this
     uint32_t vl_cap;     // neighbours per bead list
+    float ibox[3];       // 1 / box on periodic axes, 0 on the others (min_image_near)
 };
 
 // floor(n / d) for n < 2^30 and 1 <= d < 2^30 with m = floor(2^k / d) + 1,
@@ -191,6 +192,24 @@ __device__ __forceinline__ void min_image(const DevParams& P, float3& d)
         if (d.z > h) d.z -= P.box[2];
         else if (d.z < -h) d.z += P.box[2];
     }
+}
+
+// Minimum image of a separation known to be far below half the box on every
+// periodic axis (bonded neighbours, Verlet and cell-list candidates within
+// the list radius): d -= box * rint(d / box), with the rounding done by
+// adding and subtracting 1.5 * 2^23 (exact for |d / box| < 2^22), so three
+// FMA-pipe instructions per axis and no branch.  For |d| < box / 2 the shift
+// is 0 and d is unchanged; for box / 2 < |d| < box it is one box, subtracted
+// with one rounding exactly as min_image does.  The two can differ only
+// where d / box lies within rounding of +-1/2, i.e. for pairs half a box
+// apart, which no force or list of these paths reaches.  Non-periodic axes
+// have ibox = 0 and keep d.
+__device__ __forceinline__ void min_image_near(const DevParams& P, float3& d)
+{
+    constexpr float kRound = 12582912.0f;  // 1.5 * 2^23
+    d.x = fmaf(-P.box[0], fmaf(d.x, P.ibox[0], kRound) - kRound, d.x);
+    d.y = fmaf(-P.box[1], fmaf(d.y, P.ibox[1], kRound) - kRound, d.y);
+    d.z = fmaf(-P.box[2], fmaf(d.z, P.ibox[2], kRound) - kRound, d.z);
 }
 
 // floor(x / c) as the reference computes it (IEEE quotient, floor,

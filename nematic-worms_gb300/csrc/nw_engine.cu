@@ -36,6 +36,7 @@ DevParams make_dev_params(const NwConfig& c, float dt)
         P.srd_cell[a] = c.srd_cell_size[a];
         P.inv_cell[a] = 1.0f / c.cell_size[a];
         P.srd_inv_cell[a] = c.srd_cell_size[a] > 0.0f ? 1.0f / c.srd_cell_size[a] : 0.0f;
+        P.ibox[a] = c.boundary[a] == NW_PERIODIC && c.box[a] > 0.0f ? 1.0f / c.box[a] : 0.0f;
     }
     P.srd_ncells = P.srd_grid[0] * P.srd_grid[1] * P.srd_grid[2];
     P.radius = c.radius;

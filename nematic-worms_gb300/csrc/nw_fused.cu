@@ -105,7 +105,7 @@ __device__ __forceinline__ float3 wca_list_force(const DevParams& P, const float
             const uint32_t j = ids[m];
             if (j == i || lj_excluded(P, i, j, fbase)) continue;
             float3 dr = f3(__ldg(pos + j)) - r;
-            min_image(P, dr);
+            min_image_near(P, dr);
             const float rr = dot3(dr, dr);
             if (rr > P.lj_rc2) continue;
             const float fm = wca_lj(P, rr);
@@ -216,7 +216,9 @@ __device__ __forceinline__ float vl_bound(const StepBuffers& S, unsigned long lo
 // Verlet pair force: the bead's list from the last build, each pair still
 // tested against lj_rcut.  Pairs are summed in list order, which is the
 // cell-scan order of the build.  Neighbours are fetched four at a time so
-// that four index loads, then four position gathers, are in flight together.
+// that four index loads, then four position gathers, are in flight together;
+// the four pairs are evaluated without branches, a pair beyond the cut-off
+// (or past the end of the list, fetched as bead i itself) adding 0 * dr.
 __device__ __forceinline__ float3 verlet_force(const DevParams& P, const StepBuffers& S,
                                                const float4* __restrict__ pos, uint32_t i, float3 r)
 {
@@ -233,12 +235,11 @@ __device__ __forceinline__ float3 verlet_force(const DevParams& P, const StepBuf
         for (int q = 0; q < 4; ++q) pj[q] = __ldg(pos + j[q]);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            if (m + q >= k) break;
             float3 dr = f3(pj[q]) - r;
-            min_image(P, dr);
+            min_image_near(P, dr);
             const float rr = dot3(dr, dr);
-            if (rr > P.lj_rc2) continue;
-            const float fm = wca_lj(P, rr);
+            const bool in = m + q < k && rr <= P.lj_rc2;
+            const float fm = in ? wca_lj(P, rr) : 0.0f;
             f.x -= fm * dr.x;
             f.y -= fm * dr.y;
             f.z -= fm * dr.z;
@@ -270,7 +271,7 @@ __device__ __forceinline__ float3 verlet_build_force(const DevParams& P, const S
             const uint32_t j = ids[m];
             if (j == i || lj_excluded(P, i, j, fbase)) continue;
             float3 dr = f3(__ldg(pos + j)) - r;
-            min_image(P, dr);
+            min_image_near(P, dr);
             const float rr = dot3(dr, dr);
             if (rr > P.vl_r2) continue;
             if (k < P.vl_cap) col[(size_t)k * P.nb] = j;
@@ -316,6 +317,12 @@ __device__ __forceinline__ float3 list_pair_force(const DevParams& P, const Step
     }
     return wca_list_force<CAP>(P, pick2(S.pos2, cur), cnt, slots, i, r, pick2(S.hash2, cur)[i]);
 }
+
+// Resident blocks of 256 threads per SM that the WCA fused kernel is
+// compiled for (the register budget: 65536 / (256 * 6) -> 40 registers).
+#ifndef NW_FUSED_MIN_BLOCKS
+#define NW_FUSED_MIN_BLOCKS 6
+#endif
 
 // Shared-memory bytes of the pro part for a block of `beads` beads.
 __host__ __device__ __forceinline__ size_t pro_smem(uint32_t beads, bool reverse)
@@ -514,7 +521,7 @@ __global__ void __launch_bounds__(256) bead_epi_kernel(const DevParams P, const 
 
 // epi(n) then pro(n+1): the complete force of update n stays in a register.
 template <int CAP, bool kRef, int MAXT>
-__global__ void __launch_bounds__(MAXT, (MAXT == 256 && !kRef) ? 6 : 1) bead_fused_kernel(const DevParams P, const StepBuffers S, uint32_t off,
+__global__ void __launch_bounds__(MAXT, (MAXT == 256 && !kRef) ? NW_FUSED_MIN_BLOCKS : 1) bead_fused_kernel(const DevParams P, const StepBuffers S, uint32_t off,
                                                           float dt, uint32_t fpb, uint32_t pflags)
 {
     const unsigned long long n = *S.step_base + off;

@@ -420,7 +420,7 @@ __global__ void __launch_bounds__(256) pair_wca_kernel(const DevParams P, const 
             const uint32_t o = __ldg(&S.sorted_index[j]);
             if (lj_excluded(P, me, o, fbase)) continue;
             float3 dr = f3(__ldg(&S.sorted_pos[j])) - r;
-            min_image(P, dr);
+            min_image_near(P, dr);
             const float rr = dot3(dr, dr);
             if (rr > P.lj_rc2) continue;
             const float fm = wca_lj(P, rr);

@@ -133,8 +133,8 @@ __device__ __forceinline__ float div_nr(float a, float b)
 __device__ __forceinline__ Triple bend_triple(const DevParams& P, float3 ri, float3 rj, float3 rk)
 {
     float3 rij = rj - ri, rjk = rk - rj;
-    min_image(P, rij);
-    min_image(P, rjk);
+    min_image_near(P, rij);
+    min_image_near(P, rjk);
     const float qij = dot3(rij, rij), qjk = dot3(rjk, rjk);
     const float dd = dot3(rij, rjk);
     const float A = P.bend_k * (rsqrtf(qij) * rsqrtf(qjk));
@@ -151,7 +151,7 @@ __device__ __forceinline__ Triple bend_triple(const DevParams& P, float3 ri, flo
 __device__ __forceinline__ float3 tangent_of(const DevParams& P, float3 a, float3 b)
 {
     float3 rel = b - a;
-    min_image(P, rel);
+    min_image_near(P, rel);
     return rel * rsqrtf(dot3(rel, rel));
 }
 
@@ -160,7 +160,7 @@ __device__ __forceinline__ float3 tangent_of(const DevParams& P, float3 a, float
 __device__ __forceinline__ void wca_bond(const DevParams& P, float3 ri, float3 rj, float3& f)
 {
     float3 dr = rj - ri;
-    min_image(P, dr);
+    min_image_near(P, dr);
     const float q = dot3(dr, dr);
     const float ir = rsqrtf(q);
     const float fm = -(P.bond_k * (sqrt_nr(q, ir) - P.bond_r0)) * ir;
@@ -174,7 +174,7 @@ __device__ __forceinline__ void wca_bond(const DevParams& P, float3 ri, float3 r
 __device__ __forceinline__ void wca_drive(const DevParams& P, float3 ri, float3 rn, float3& f)
 {
     float3 dr = rn - ri;
-    min_image(P, dr);
+    min_image_near(P, dr);
     const float s = P.activity * rsqrtf(dot3(dr, dr));
     f.x += s * dr.x;
     f.y += s * dr.y;
@@ -186,7 +186,7 @@ __device__ __forceinline__ void wca_drive(const DevParams& P, float3 ri, float3 
 __device__ __forceinline__ void wca_bond_drive(const DevParams& P, float3 ri, float3 rn, float3& f)
 {
     float3 dr = rn - ri;
-    min_image(P, dr);
+    min_image_near(P, dr);
     const float q = dot3(dr, dr);
     const float ir = rsqrtf(q);
     const float fm = -(P.bond_k * (sqrt_nr(q, ir) - P.bond_r0)) * ir;
