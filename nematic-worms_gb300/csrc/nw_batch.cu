@@ -49,6 +49,7 @@ struct nw_batch {
     uint64_t step = 0, version = 1, last_launches = 0;
     bool use_graphs = true, vl = false, vl_dirty = true, lists_dirty = true;
     bool tan_stale = false;  // tangents of lazy replicas (pro_flags) computed when read
+    bool planar = false;     // every replica is two-dimensional (the planar kernels)
     std::vector<BatchGraph> graphs;
 };
 
@@ -186,7 +187,10 @@ cudaError_t clean(nw_batch* b)
     }
     if (b->vl && b->vl_dirty) {
         std::vector<uint32_t> init(8ull * b->R, 0u);
-        for (int r = 0; r < b->R; ++r) init[8ull * r] = init[8ull * r + 1] = 0x7f000000u;
+        for (int r = 0; r < b->R; ++r) {
+            init[8ull * r] = init[8ull * r + 1] = 0x7f000000u;  // a list build at the first pair pass
+            init[8ull * r + 6] = 7u;                            // every count buffer counts as filled
+        }
         // pageable source: the copy is staged before the call returns
         e = cudaMemcpyAsync(b->B.vstate, init.data(), init.size() * 4, cudaMemcpyHostToDevice, b->stream);
         if (e != cudaSuccess) return e;
@@ -200,7 +204,8 @@ uint64_t enqueue(nw_batch* b, int nsteps)
     if (b->blocks == 0) return 0;
     uint64_t launches = 0;
     auto L = [&](int mode, uint32_t off) {
-        launch_batch(mode, b->d_slots, b->d_block_rep, b->blocks, b->threads, b->smem, b->cap, b->B, off, b->stream);
+        launch_batch(mode, b->d_slots, b->d_block_rep, b->blocks, b->threads, b->smem, b->cap, b->B, off, b->planar,
+                     b->stream);
         ++launches;
     };
     L(kBatchPro, 0u);
@@ -294,6 +299,8 @@ nw_status nw_batch_create(const NwConfig* replicas, int n, nw_batch** out)
     nw_batch* b = new nw_batch();
     b->cfg.assign(replicas, replicas + n);
     b->R = n;
+    b->planar = true;
+    for (int r = 0; r < n; ++r) b->planar = b->planar && replicas[r].dim == 2;  // all are WCA worms
     if (cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete b;
         return NW_ERR_CUDA;

@@ -59,6 +59,14 @@ struct DevParams {
     float ibox[3];       // 1 / box on periodic axes, 0 on the others (min_image_near)
 };
 
+// Planar systems (two-dimensional WCA worms) compute with two vector
+// components, as the archived two-dimensional worm kernels do; their step
+// kernels are compiled for D = 2 (planar arithmetic below).
+__host__ __device__ __forceinline__ bool planar_system(const DevParams& P)
+{
+    return P.model == NW_MODEL_WCA_WORMS && P.dim == 2;
+}
+
 // floor(n / d) for n < 2^30 and 1 <= d < 2^30 with m = floor(2^k / d) + 1,
 // k = 30 + ceil(log2 d): n * m / 2^k = n / d + e with 0 < e < 1 / d
 // (Granlund and Montgomery, "Division by invariant integers using
@@ -88,6 +96,54 @@ __device__ __forceinline__ void operator+=(float3& a, float3 b) { a.x += b.x; a.
 __device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ float3 zero3() { return make_float3(0.f, 0.f, 0.f); }
 __device__ __forceinline__ bool finite3(float3 a) { return isfinite(a.x) && isfinite(a.y) && isfinite(a.z); }
+
+// ---- planar arithmetic -------------------------------------------------------
+// Two-dimensional WCA worm systems compute in the xy plane, as the archived
+// worm kernels do with two components per vector (NWWormsKernel_*.h, built
+// with _D_ = 2).  With D = 2 the helpers below drop every z operation: a
+// bead's z coordinate and velocity are carried unchanged and its forces have
+// z = 0.  D = 3 is the three-component arithmetic of the other systems.
+template <int D>
+__device__ __forceinline__ float dotv(float3 a, float3 b)
+{
+    if constexpr (D == 2) return a.x * b.x + a.y * b.y;
+    else return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+// a - b (z = 0 for D = 2)
+template <int D>
+__device__ __forceinline__ float3 subv(float3 a, float3 b)
+{
+    if constexpr (D == 2) return make_float3(a.x - b.x, a.y - b.y, 0.f);
+    else return make_float3(a.x - b.x, a.y - b.y, a.z - b.z);
+}
+// s a (z = 0 for D = 2)
+template <int D>
+__device__ __forceinline__ float3 scalev(float s, float3 a)
+{
+    if constexpr (D == 2) return make_float3(s * a.x, s * a.y, 0.f);
+    else return make_float3(s * a.x, s * a.y, s * a.z);
+}
+// a + b (a's z for D = 2)
+template <int D>
+__device__ __forceinline__ float3 addv(float3 a, float3 b)
+{
+    if constexpr (D == 2) return make_float3(a.x + b.x, a.y + b.y, a.z);
+    else return make_float3(a.x + b.x, a.y + b.y, a.z + b.z);
+}
+// f -= s a, component by component (f's z untouched for D = 2)
+template <int D>
+__device__ __forceinline__ void sub_scaled(float3& f, float s, float3 a)
+{
+    f.x -= s * a.x;
+    f.y -= s * a.y;
+    if constexpr (D == 3) f.z -= s * a.z;
+}
+template <int D>
+__device__ __forceinline__ bool finitev(float3 a)
+{
+    if constexpr (D == 2) return isfinite(a.x) && isfinite(a.y);
+    else return isfinite(a.x) && isfinite(a.y) && isfinite(a.z);
+}
 
 // ---- Philox4x32-10 (Salmon et al., SC'11) ----------------------------------
 __host__ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1)
@@ -204,12 +260,13 @@ __device__ __forceinline__ void min_image(const DevParams& P, float3& d)
 // where d / box lies within rounding of +-1/2, i.e. for pairs half a box
 // apart, which no force or list of these paths reaches.  Non-periodic axes
 // have ibox = 0 and keep d.
+template <int D = 3>
 __device__ __forceinline__ void min_image_near(const DevParams& P, float3& d)
 {
     constexpr float kRound = 12582912.0f;  // 1.5 * 2^23
     d.x = fmaf(-P.box[0], fmaf(d.x, P.ibox[0], kRound) - kRound, d.x);
     d.y = fmaf(-P.box[1], fmaf(d.y, P.ibox[1], kRound) - kRound, d.y);
-    d.z = fmaf(-P.box[2], fmaf(d.z, P.ibox[2], kRound) - kRound, d.z);
+    if constexpr (D == 3) d.z = fmaf(-P.box[2], fmaf(d.z, P.ibox[2], kRound) - kRound, d.z);
 }
 
 // floor(x / c) as the reference computes it (IEEE quotient, floor,
@@ -318,13 +375,15 @@ __device__ __forceinline__ uint32_t srd_hash(const DevParams& P, float3 p, float
 }
 
 // periodicBoundary / dampedWallBoundary / noslipWallBoundary in
-// filament_integrator's axis order (particles_kernel_impl.cuh:34-68, 99-134).
+// filament_integrator's axis order (particles_kernel_impl.cuh:34-68, 99-134);
+// planar systems (D = 2) leave the z axis alone.
+template <int D = 3>
 __device__ __forceinline__ void apply_boundaries(const DevParams& P, float3& p, float3& v, float3 dr, float rad)
 {
     float* pp = &p.x;
     float* vv = &v.x;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
+    for (int a = 0; a < D; ++a) {
         const float L0 = P.origin[a], L = P.box[a];
         const int b = P.bnd[a];
         if (b == NW_PERIODIC) {
@@ -352,7 +411,7 @@ __device__ __forceinline__ void apply_boundaries(const DevParams& P, float3& p, 
                 p = p - dr;
                 pp[a] = target;
                 const float nx = a == 0 ? 1.f : 0.f, ny = a == 1 ? 1.f : 0.f;
-                v = make_float3(-v.x * nx, -v.y * ny, -v.z * 0.f);
+                v = make_float3(-v.x * nx, -v.y * ny, D == 3 ? -v.z * 0.f : v.z);
             }
         }
     }

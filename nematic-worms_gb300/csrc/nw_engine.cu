@@ -325,8 +325,9 @@ uint32_t collision_parity(const nw_system* s, uint64_t first, int nsteps)
 cudaError_t clean_lists(nw_system* s)
 {
     if (s->vl && s->vl_dirty) {
-        // an unbounded displacement forces a list build at the next pair pass
-        const uint32_t init[8] = {0x7f000000u, 0x7f000000u, 0u, 0u, 0u, 0u, 0u, 0u};
+        // an unbounded displacement forces a list build at the next pair pass;
+        // every cell-list count buffer counts as filled (word 6)
+        const uint32_t init[8] = {0x7f000000u, 0x7f000000u, 0u, 0u, 0u, 0u, 7u, 0u};
         cudaError_t e = cudaMemcpyAsync(s->B.vstate, init, sizeof(init), cudaMemcpyHostToDevice, s->stream);
         if (e != cudaSuccess) return e;
         s->vl_dirty = false;

@@ -52,8 +52,18 @@ struct ReplicaSlot {
 enum BatchMode { kBatchPro = 0, kBatchEpi = 1, kBatchFused = 2, kBatchList = 3 };
 
 // One launch over all replicas: block b serves replica block_rep[b].  S holds
-// the batch's base pointers; `threads` >= every replica's fpb * L.
+// the batch's base pointers; `threads` >= every replica's fpb * L; planar =
+// every replica is a planar system.
 void launch_batch(int mode, const ReplicaSlot* table, const uint32_t* block_rep, uint32_t blocks, uint32_t threads,
-                  size_t smem, uint32_t cap, const StepBuffers& S, uint32_t off, cudaStream_t s);
+                  size_t smem, uint32_t cap, const StepBuffers& S, uint32_t off, bool planar, cudaStream_t s);
+
+// The two-component launches (nw_fused_planar.cu) behind the launchers above.
+uint64_t launch_bead_pro_planar(const DevParams& P, const StepBuffers& B, uint32_t off, float dt, cudaStream_t s);
+uint64_t launch_bead_tangents_planar(const DevParams& P, const float4* pos, float4* tan, cudaStream_t s);
+uint64_t launch_bead_epi_planar(const DevParams& P, const StepBuffers& B, uint32_t off, cudaStream_t s);
+uint64_t launch_bead_fused_planar(const DevParams& P, const StepBuffers& B, uint32_t off, float dt, cudaStream_t s);
+void launch_batch_planar(int mode, const ReplicaSlot* table, const uint32_t* block_rep, uint32_t blocks,
+                         uint32_t threads, size_t smem, uint32_t cap, const StepBuffers& S, uint32_t off,
+                         cudaStream_t s);
 
 }  // namespace nw

@@ -4,8 +4,12 @@
 
 namespace nw {
 
-__global__ void __launch_bounds__(1024) filament_pass_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
-                                                             float dt, uint32_t fpb)
+namespace {
+
+// The filament pass with D vector components (D = 2: planar systems).
+template <int D>
+__device__ __forceinline__ void filament_pass(const DevParams& P, const StepBuffers& S, uint32_t step_off, float dt,
+                                              uint32_t fpb)
 {
     extern __shared__ float4 sm[];
     const uint32_t L = P.L;
@@ -21,15 +25,21 @@ __global__ void __launch_bounds__(1024) filament_pass_kernel(const DevParams P, 
         const float4 P4 = S.pos[i], V4 = S.vel[i], F4 = S.force[i], Fo4 = S.force_old[i];
         float3 p = f3(P4), v = f3(V4);
         const float3 f = f3(F4), fo = f3(Fo4);
-        // velocity Verlet (particles_kernel_impl.cuh:93-97)
-        const float3 dv = (0.5f * (f + fo)) * dt;
-        v += dv;
-        const float3 dr = v * dt + ((0.5f * f) * dt) * dt;
-        p += dr;
-        apply_boundaries(P, p, v, dr, P.radius);
+        // velocity Verlet (particles_kernel_impl.cuh:93-97), per axis
+        auto verlet = [dt](float fa, float foa, float& va, float& pa) {
+            va += (0.5f * (fa + foa)) * dt;
+            const float d = va * dt + ((0.5f * fa) * dt) * dt;
+            pa += d;
+            return d;
+        };
+        float3 dr;
+        dr.x = verlet(f.x, fo.x, v.x, p.x);
+        dr.y = verlet(f.y, fo.y, v.y, p.y);
+        dr.z = D == 3 ? verlet(f.z, fo.z, v.z, p.z) : 0.f;
+        apply_boundaries<D>(P, p, v, dr, P.radius);
         nP = make_float4(p.x, p.y, p.z, P4.w);
         nV = make_float4(v.x, v.y, v.z, V4.w);
-        nFo = make_float4(f.x, f.y, f.z, Fo4.w);
+        nFo = make_float4(f.x, f.y, D == 3 ? f.z : 0.f, Fo4.w);
     }
     if (P.reverse_on) {
         // reverseFilamentsKernel (particles_kernel_impl.cuh:820-857)
@@ -63,45 +73,54 @@ __global__ void __launch_bounds__(1024) filament_pass_kernel(const DevParams P, 
         const float3 g = noise3(P, rng_draw(P, i, step, kRngLangevin));
         float3 fl = zero3() - P.gamma * f3(nV);
         fl += g;
-        fs = fl;
+        fs = D == 3 ? fl : make_float3(fl.x, fl.y, 0.f);
     }
     // bending contributions in the reference's triple order p = c-2, c-1, c
     if (L >= 3) {
-        if (c >= 2) fs += bend_triple(P, f3(R[c - 2]), f3(R[c - 1]), f3(R[c])).fk;
-        if (c >= 1 && c + 1 < L) fs += bend_triple(P, f3(R[c - 1]), f3(R[c]), f3(R[c + 1])).fj;
-        if (c + 2 < L) fs += bend_triple(P, f3(R[c]), f3(R[c + 1]), f3(R[c + 2])).fi;
+        if (c >= 2) fs = addv<D>(fs, bend_triple<D>(P, f3(R[c - 2]), f3(R[c - 1]), f3(R[c])).fk);
+        if (c >= 1 && c + 1 < L) fs = addv<D>(fs, bend_triple<D>(P, f3(R[c - 1]), f3(R[c]), f3(R[c + 1])).fj);
+        if (c + 2 < L) fs = addv<D>(fs, bend_triple<D>(P, f3(R[c]), f3(R[c + 1]), f3(R[c + 2])).fi);
     }
     bool wt = false;
     float3 tg = zero3();
     if (L >= 3) {
         if (c == 0) {
-            tg = tangent_of(P, f3(R[0]), f3(R[1]));
+            tg = tangent_of<D>(P, f3(R[0]), f3(R[1]));
             wt = true;
         } else if (c == L - 1) {
             if (L > 3) {
-                tg = tangent_of(P, f3(R[L - 2]), f3(R[L - 1]));
+                tg = tangent_of<D>(P, f3(R[L - 2]), f3(R[L - 1]));
                 wt = true;
             }
         } else {
-            tg = tangent_of(P, f3(R[c - 1]), f3(R[c + 1]));
+            tg = tangent_of<D>(P, f3(R[c - 1]), f3(R[c + 1]));
             wt = true;
         }
     }
     if (P.model == NW_MODEL_WCA_WORMS) {
         const float3 me = f3(R[c]);
-        if (c > 0) wca_bond(P, me, f3(R[c - 1]), fs);
-        if (c + 1 < L) wca_bond_drive(P, me, f3(R[c + 1]), fs);
+        if (c > 0) wca_bond<D>(P, me, f3(R[c - 1]), fs);
+        if (c + 1 < L) wca_bond_drive<D>(P, me, f3(R[c + 1]), fs);
     }
     S.pos[i] = nP;
     S.vel[i] = nV;
     S.force_old[i] = nFo;
     S.force[i] = make_float4(fs.x, fs.y, fs.z, 0.f);
     if (wt) S.tangent[i] = make_float4(tg.x, tg.y, tg.z, 0.f);
-    if (!finite3(f3(nP)) || !finite3(fs)) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
+    if (!finitev<D>(f3(nP)) || !finitev<D>(fs)) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
 
     const uint32_t h = bead_hash(P, f3(nP));
     S.hash[i] = h;
     S.slot[i] = count_into_cell(S.cell_count, h);
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(1024) filament_pass_kernel(const DevParams P, const StepBuffers S, uint32_t step_off,
+                                                             float dt, uint32_t fpb)
+{
+    if (planar_system(P)) filament_pass<2>(P, S, step_off, dt, fpb);
+    else filament_pass<3>(P, S, step_off, dt, fpb);
 }
 
 __global__ void __launch_bounds__(512) chunk_sum_kernel(const uint32_t* __restrict__ a, uint32_t m,
@@ -400,7 +419,11 @@ __global__ void __launch_bounds__(kRefThreads) pair_ref_tiled_kernel(const DevPa
     }
 }
 
-__global__ void __launch_bounds__(256) pair_wca_kernel(const DevParams P, const StepBuffers S)
+namespace {
+
+// WCA pair forces from the sorted arrays with D vector components.
+template <int D>
+__device__ __forceinline__ void pair_wca(const DevParams& P, const StepBuffers& S)
 {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P.nb) return;
@@ -419,22 +442,27 @@ __global__ void __launch_bounds__(256) pair_wca_kernel(const DevParams P, const 
             if (j == p) continue;
             const uint32_t o = __ldg(&S.sorted_index[j]);
             if (lj_excluded(P, me, o, fbase)) continue;
-            float3 dr = f3(__ldg(&S.sorted_pos[j])) - r;
-            min_image_near(P, dr);
-            const float rr = dot3(dr, dr);
+            float3 dr = subv<D>(f3(__ldg(&S.sorted_pos[j])), r);
+            min_image_near<D>(P, dr);
+            const float rr = dotv<D>(dr, dr);
             if (rr > P.lj_rc2) continue;
-            const float fm = wca_lj(P, rr);
-            f.x -= fm * dr.x;
-            f.y -= fm * dr.y;
-            f.z -= fm * dr.z;
+            sub_scaled<D>(f, wca_lj(P, rr), dr);
         }
     });
     float4 F = S.force[me];
     F.x += f.x;
     F.y += f.y;
-    F.z += f.z;
+    if constexpr (D == 3) F.z += f.z;
     S.force[me] = F;
-    if (!finite3(f3(F))) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
+    if (!finitev<D>(f3(F))) atomicOr(S.err, (uint32_t)NW_EFLAG_NONFINITE);
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(256) pair_wca_kernel(const DevParams P, const StepBuffers S)
+{
+    if (planar_system(P)) pair_wca<2>(P, S);
+    else pair_wca<3>(P, S);
 }
 
 // SRD cell hash of every particle (beads from the current bead buffer,

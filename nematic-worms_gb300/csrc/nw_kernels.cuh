@@ -47,7 +47,9 @@ struct StepBuffers {
     // Verlet lists (vl_on): neighbours of bead i in nbr[k * nb + i], k < nnb[i];
     // vstate[0..1] displacement bound of the state after update n in [n & 1],
     // vstate[2..4] maximum bead displacement of update n in [2 + n % 3]
-    // (float bits; the bound counts from the last list build)
+    // (float bits; the bound counts from the last list build), vstate[5] the
+    // largest move of positions set from the host, vstate[6] bit b set while
+    // lcount[b] holds entries of a list build
     uint32_t *nbr, *nnb, *vstate;
     uint32_t *cell_count, *cell_offset, *cell_start, *cell_end, *chunk_count;
     float4 *sorted_pos, *sorted_vel, *sorted_tan;
@@ -130,70 +132,74 @@ __device__ __forceinline__ float div_nr(float a, float b)
 // One bending triple (filamentKernel, particles_kernel_impl.cuh:777-800):
 // A = k_b / (d_ij d_jk), F_i = -A (r_jk - r_ij (r_ij . r_jk) / d_ij^2),
 // F_k = -A (r_jk (r_ij . r_jk) / d_jk^2 - r_ij), F_j = -F_i - F_k.
+// D = 2: in the xy plane (planar arithmetic, nw_device.cuh).
+template <int D = 3>
 __device__ __forceinline__ Triple bend_triple(const DevParams& P, float3 ri, float3 rj, float3 rk)
 {
-    float3 rij = rj - ri, rjk = rk - rj;
-    min_image_near(P, rij);
-    min_image_near(P, rjk);
-    const float qij = dot3(rij, rij), qjk = dot3(rjk, rjk);
-    const float dd = dot3(rij, rjk);
+    float3 rij = subv<D>(rj, ri), rjk = subv<D>(rk, rj);
+    min_image_near<D>(P, rij);
+    min_image_near<D>(P, rjk);
+    const float qij = dotv<D>(rij, rij), qjk = dotv<D>(rjk, rjk);
+    const float dd = dotv<D>(rij, rjk);
     const float A = P.bend_k * (rsqrtf(qij) * rsqrtf(qjk));
-    const float3 B = rij * div_nr(dd, qij);
-    const float3 C = rjk * div_nr(dd, qjk);
+    const float3 B = scalev<D>(div_nr(dd, qij), rij);
+    const float3 C = scalev<D>(div_nr(dd, qjk), rjk);
     Triple t;
-    t.fi = (-A) * (rjk - B);
-    t.fk = (-A) * (C - rij);
-    t.fj = (-t.fi) - t.fk;
+    t.fi = scalev<D>(-A, subv<D>(rjk, B));
+    t.fk = scalev<D>(-A, subv<D>(C, rij));
+    t.fj = subv<D>(make_float3(-t.fi.x, -t.fi.y, -t.fi.z), t.fk);
     return t;
 }
 
 // getTangent (particles_kernel_impl.cuh:303-309): the unit vector a -> b.
+template <int D = 3>
 __device__ __forceinline__ float3 tangent_of(const DevParams& P, float3 a, float3 b)
 {
-    float3 rel = b - a;
-    min_image_near(P, rel);
-    return rel * rsqrtf(dot3(rel, rel));
+    float3 rel = subv<D>(b, a);
+    min_image_near<D>(P, rel);
+    return scalev<D>(rsqrtf(dotv<D>(rel, rel)), rel);
 }
 
 // Archived harmonic bond (NWWormsKernel_InternalForce.h:37-59):
 // F_i = k (|r| - r0) r / |r| with r = r_j - r_i.
+template <int D = 3>
 __device__ __forceinline__ void wca_bond(const DevParams& P, float3 ri, float3 rj, float3& f)
 {
-    float3 dr = rj - ri;
-    min_image_near(P, dr);
-    const float q = dot3(dr, dr);
+    float3 dr = subv<D>(rj, ri);
+    min_image_near<D>(P, dr);
+    const float q = dotv<D>(dr, dr);
     const float ir = rsqrtf(q);
     const float fm = -(P.bond_k * (sqrt_nr(q, ir) - P.bond_r0)) * ir;
-    f.x -= fm * dr.x;
-    f.y -= fm * dr.y;
-    f.z -= fm * dr.z;
+    sub_scaled<D>(f, fm, dr);
 }
 
 // Archived tangent drive (NWWormsKernel_DriveForce.h:21-34): F_act along
 // the unit vector to the next bead.
+template <int D = 3>
 __device__ __forceinline__ void wca_drive(const DevParams& P, float3 ri, float3 rn, float3& f)
 {
-    float3 dr = rn - ri;
-    min_image_near(P, dr);
-    const float s = P.activity * rsqrtf(dot3(dr, dr));
+    float3 dr = subv<D>(rn, ri);
+    min_image_near<D>(P, dr);
+    const float s = P.activity * rsqrtf(dotv<D>(dr, dr));
     f.x += s * dr.x;
     f.y += s * dr.y;
-    f.z += s * dr.z;
+    if constexpr (D == 3) f.z += s * dr.z;
 }
 
 // The bond to the next bead and the drive along it share one separation
 // and one reciprocal square root.
+template <int D = 3>
 __device__ __forceinline__ void wca_bond_drive(const DevParams& P, float3 ri, float3 rn, float3& f)
 {
-    float3 dr = rn - ri;
-    min_image_near(P, dr);
-    const float q = dot3(dr, dr);
+    float3 dr = subv<D>(rn, ri);
+    min_image_near<D>(P, dr);
+    const float q = dotv<D>(dr, dr);
     const float ir = rsqrtf(q);
     const float fm = -(P.bond_k * (sqrt_nr(q, ir) - P.bond_r0)) * ir;
     const float s = P.activity * ir;
     f.x += s * dr.x - fm * dr.x;
     f.y += s * dr.y - fm * dr.y;
-    f.z += s * dr.z - fm * dr.z;
+    if constexpr (D == 3) f.z += s * dr.z - fm * dr.z;
 }
 
 // Repulsive LJ magnitude of NWWormsKernel_LennardJones.h:38-50,

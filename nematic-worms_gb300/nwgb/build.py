@@ -39,7 +39,7 @@ def reference_tree() -> Path | None:
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 
-CU_SOURCES = ["nw_kernels.cu", "nw_fused.cu", "nw_engine.cu", "nw_legacy.cu", "nw_sort.cu", "nw_noalloc.cu", "nw_batch.cu", "nw_adjoint.cu", "nw_writer.cu", "nw_defects.cu", "nw_observables.cu"]
+CU_SOURCES = ["nw_kernels.cu", "nw_fused.cu", "nw_fused_planar.cu", "nw_engine.cu", "nw_legacy.cu", "nw_sort.cu", "nw_noalloc.cu", "nw_batch.cu", "nw_adjoint.cu", "nw_writer.cu", "nw_defects.cu", "nw_observables.cu"]
 CPP_SOURCES = ["nw_config.cpp"]
 
 

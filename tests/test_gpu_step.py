@@ -301,6 +301,28 @@ def test_graph_replay_is_bit_identical_to_direct_launches(lib, kind, strategy):
         assert np.array_equal(a[k], c[k]), k  # run twice: no races
 
 
+@pytest.mark.parametrize("strategy", STRATEGIES)
+def test_planar_system_carries_z(lib, strategy):
+    """Two-dimensional WCA worms compute in the xy plane, with the two vector
+    components of the archived worm kernels: beads given z offsets and z
+    velocities follow the same xy trajectory bit for bit, keep their z and z
+    velocity, and take no z force."""
+    cfg, pos, vel, tan = make_case("wca", lib)
+    assert cfg.dim == 2 and cfg.model == abi.NW_MODEL_WCA_WORMS
+    cfg.strategy = strategy
+    a = run_gpu(cfg, pos, vel, tan, nsteps=12)
+    rng = np.random.default_rng(3)
+    pz, vz = pos.copy(), vel.copy()
+    pz[:, 2] = rng.uniform(-0.4, 0.4, len(pz)).astype(np.float32)  # inside the z extent: no wrap
+    vz[:, 2] = rng.normal(0.0, 0.5, len(vz)).astype(np.float32)
+    b = run_gpu(cfg, pz, vz, tan, nsteps=12)
+    for k in ("pos", "vel", "force", "force_old"):
+        assert np.array_equal(a[k][:, :2], b[k][:, :2]), k
+    assert np.array_equal(b["pos"][:, 2], pz[:, 2])
+    assert np.array_equal(b["vel"][:, 2], vz[:, 2])
+    assert np.all(b["force"][:, 2] == 0) and np.all(b["force_old"][:, 2] == 0)
+
+
 @pytest.mark.parametrize("kind", ["wca", "wca_srd", "ref"])
 def test_strategies_agree(lib, orc, kind):
     """Cell lists visit each cell's beads in index order, as the sorted
