@@ -762,6 +762,7 @@ def batch_block(args, steps=None):
                        "graph_steps": chunk, "parallelism": f"replicas x{world}",
                        "tuning": {"threads_per_block": tune.threads_per_block, "strategy": int(tune.strategy),
                                   "neighbor_skin": round(float(tune.neighbor_skin), 3),
+                                  "cell_capacity": int(tune.cell_capacity),
                                   "autotune_ms_per_step": float(tune.ms_per_step)},
                        "l2": "state larger than L2 (no flush needed)"},
             "clocks": clk, "gpu_launches": launches,

@@ -30,15 +30,20 @@ typedef struct nw_batch nw_batch;
 /* Launch shape and neighbour search of a batch (what the autotuner picks).
  *  threads_per_block  block size; each block holds whole filaments of one
  *                     replica (128, 256 or 512)
- *  strategy           NW_STRATEGY_VERLET or NW_STRATEGY_CELL_LISTS
+ *  strategy           NW_STRATEGY_VERLET or NW_STRATEGY_CELL_LISTS (the
+ *                     sort-free orderings; the sorted scheme is single-system)
  *  neighbor_skin      Verlet skin (sets the list-cell size lj_rcut + skin)
  *  ms_per_step        measured time of one step of the whole batch (output
- *                     of nw_batch_autotune; ignored on input) */
+ *                     of nw_batch_autotune; ignored on input)
+ *  cell_capacity      slots per list cell, 8 or 16 (0 on input: 16 if any
+ *                     replica's cell_capacity asks for it, else 8; the
+ *                     value in use on output) */
 typedef struct NwBatchTuning {
     uint32_t threads_per_block;
     int32_t strategy;
     float neighbor_skin;
     float ms_per_step;
+    uint32_t cell_capacity;
 } NwBatchTuning;
 
 /* Create a batch of n replicas from their configurations (each validated as
@@ -76,10 +81,17 @@ nw_status nw_batch_get_tuning(const nw_batch* b, NwBatchTuning* t);
 nw_status nw_batch_set_tuning(nw_batch* b, const NwBatchTuning* t);
 
 /* Time trial_steps steps of every candidate (block sizes 128, 256, 512;
- * Verlet lists with skins 0.2, 0.3, 0.45 sigma and plain cell lists), each
- * from the same saved state, keep the fastest and restore the state.
+ * Verlet lists with skins 0.2, 0.3, 0.45 sigma and plain cell lists; 8 or
+ * 16 slots per list cell), each from the same saved state, keep the fastest
+ * and restore the state.  A candidate whose cells overflow is skipped.  The
+ * result is cached for the batch's class: total beads by powers of two and
+ * mean packing fraction (beads x pi sigma^2 / 4 over the box area; volume
+ * fraction in 3D) by steps of 0.05.  trial_steps = 0 takes the cached tuning
+ * of the class without timing when there is one (else times 20 steps).
  * Writes the chosen tuning (with its time) to *chosen if not NULL. */
 nw_status nw_batch_autotune(nw_batch* b, int trial_steps, NwBatchTuning* chosen);
+/* The (bead-count, packing) class of the batch that keys the tuning cache. */
+nw_status nw_batch_tuning_class(const nw_batch* b, int* bead_class, int* packing_class);
 
 #ifdef __cplusplus
 }

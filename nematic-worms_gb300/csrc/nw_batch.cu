@@ -9,6 +9,8 @@
 // pro / epi / fused step bodies as a single system (nw_fused.cu).
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "../../include/nwgb_batch.h"
@@ -55,6 +57,59 @@ struct nw_batch {
 
 namespace {
 
+// ---- tuning cache: one tuning per (bead-count, packing) class of batches ----
+struct TuneKey {
+    int beads;    // floor(log2(total beads))
+    int packing;  // floor(mean packing fraction / 0.05)
+};
+
+TuneKey tune_key(const nw_batch* b)
+{
+    TuneKey k{0, 0};
+    uint64_t n = b->total;
+    while (n > 1) {
+        n >>= 1;
+        ++k.beads;
+    }
+    constexpr double kPi = 3.14159265358979323846;
+    double phi = 0.0;
+    for (const auto& c : b->cfg) {
+        const double s = c.lj_sigma, nb = (double)c.num_filaments * c.filament_size;
+        if (c.dim >= 3)
+            phi += nb * (kPi / 6.0) * s * s * s / ((double)c.box[0] * c.box[1] * c.box[2]);
+        else
+            phi += nb * (kPi / 4.0) * s * s / ((double)c.box[0] * c.box[1]);
+    }
+    if (!b->cfg.empty()) phi /= (double)b->cfg.size();
+    k.packing = (int)std::floor(phi / 0.05);
+    return k;
+}
+
+std::mutex g_tune_mutex;
+std::vector<std::pair<TuneKey, NwBatchTuning>> g_tune_cache;
+
+bool tune_cache_find(const TuneKey& k, NwBatchTuning* t)
+{
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    for (const auto& e : g_tune_cache)
+        if (e.first.beads == k.beads && e.first.packing == k.packing) {
+            *t = e.second;
+            return true;
+        }
+    return false;
+}
+
+void tune_cache_store(const TuneKey& k, const NwBatchTuning& t)
+{
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    for (auto& e : g_tune_cache)
+        if (e.first.beads == k.beads && e.first.packing == k.packing) {
+            e.second = t;
+            return;
+        }
+    g_tune_cache.push_back({k, t});
+}
+
 nw_status cuda_st(cudaError_t e)
 {
     if (e == cudaSuccess) return NW_OK;
@@ -96,6 +151,7 @@ nw_status configure(nw_batch* b, const NwBatchTuning& t)
     if (t.threads_per_block != 128 && t.threads_per_block != 256 && t.threads_per_block != 512) return NW_ERR_INVALID;
     if (t.strategy != NW_STRATEGY_VERLET && t.strategy != NW_STRATEGY_CELL_LISTS) return NW_ERR_INVALID;
     if (!(t.neighbor_skin >= 0.0f) || !std::isfinite(t.neighbor_skin)) return NW_ERR_INVALID;
+    if (t.cell_capacity != 0 && t.cell_capacity != 8 && t.cell_capacity != 16) return NW_ERR_INVALID;
     cudaStreamSynchronize(b->stream);
     drop_graphs(b);
     free_list(b->list_allocs);
@@ -107,6 +163,7 @@ nw_status configure(nw_batch* b, const NwBatchTuning& t)
         reverse |= c.reverse_probability > 0.0f;
         if (c.cell_capacity == 16) b->cap = 16;
     }
+    if (t.cell_capacity) b->cap = t.cell_capacity;
     uint32_t threads = t.threads_per_block;
     const uint32_t need = (maxL + 31u) & ~31u;
     if (need > threads) threads = need;
@@ -166,7 +223,7 @@ nw_status configure(nw_batch* b, const NwBatchTuning& t)
         e = cudaMemcpy(b->d_block_rep, block_rep.data(), block_rep.size() * 4, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_st(e);
     b->tune = t;
-    b->tune.threads_per_block = t.threads_per_block;
+    b->tune.cell_capacity = b->cap;
     b->version++;
     b->lists_dirty = true;
     b->vl_dirty = true;
@@ -522,9 +579,30 @@ nw_status nw_batch_set_tuning(nw_batch* b, const NwBatchTuning* t)
     return st;
 }
 
+nw_status nw_batch_tuning_class(const nw_batch* b, int* bead_class, int* packing_class)
+{
+    if (!b) return NW_ERR_INVALID;
+    const TuneKey k = tune_key(b);
+    if (bead_class) *bead_class = k.beads;
+    if (packing_class) *packing_class = k.packing;
+    return NW_OK;
+}
+
 nw_status nw_batch_autotune(nw_batch* b, int trial_steps, NwBatchTuning* chosen)
 {
-    if (!b || trial_steps < 2) return NW_ERR_INVALID;
+    if (!b || trial_steps < 0 || trial_steps == 1) return NW_ERR_INVALID;
+    const TuneKey key = tune_key(b);
+    if (trial_steps == 0) {
+        NwBatchTuning cached;
+        if (tune_cache_find(key, &cached)) {
+            nw_status st = configure(b, cached);
+            if (st != NW_OK) return st;
+            b->tune.ms_per_step = cached.ms_per_step;
+            if (chosen) *chosen = b->tune;
+            return NW_OK;
+        }
+        trial_steps = 20;
+    }
     cudaError_t e = cudaStreamSynchronize(b->stream);
     if (e != cudaSuccess) return cuda_st(e);
     // saved state: the current buffers of position, velocity, tangent, force, old force
@@ -558,37 +636,49 @@ nw_status nw_batch_autotune(nw_batch* b, int trial_steps, NwBatchTuning* chosen)
     NwBatchTuning best = start;
     best.ms_per_step = INFINITY;
     const uint32_t threads[3] = {128u, 256u, 512u};
-    const NwBatchTuning searches[4] = {{0, NW_STRATEGY_VERLET, 0.2f, 0}, {0, NW_STRATEGY_VERLET, 0.3f, 0},
-                                       {0, NW_STRATEGY_VERLET, 0.45f, 0}, {0, NW_STRATEGY_CELL_LISTS, 0.3f, 0}};
+    const uint32_t caps[2] = {8u, 16u};
+    const NwBatchTuning searches[4] = {{0, NW_STRATEGY_VERLET, 0.2f, 0, 0}, {0, NW_STRATEGY_VERLET, 0.3f, 0, 0},
+                                       {0, NW_STRATEGY_VERLET, 0.45f, 0, 0}, {0, NW_STRATEGY_CELL_LISTS, 0.3f, 0, 0}};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEventCreate(&ev0);
     cudaEventCreate(&ev1);
     for (int a = 0; a < 3 && st == NW_OK; ++a)
-        for (int s = 0; s < 4 && st == NW_OK; ++s) {
-            NwBatchTuning t = searches[s];
-            t.threads_per_block = threads[a];
-            // a candidate the replicas cannot run (e.g. lists too large) is skipped
-            if (configure(b, t) != NW_OK) continue;
-            st = restore();
-            if (st == NW_OK) st = nw_batch_step(b, trial_steps);  // capture + warm
-            if (st == NW_OK) st = nw_batch_sync(b);
-            if (st == NW_OK) st = restore();
-            if (st != NW_OK) break;
-            cudaEventRecord(ev0, b->stream);
-            st = nw_batch_step(b, trial_steps);
-            cudaEventRecord(ev1, b->stream);
-            if (st == NW_OK) st = nw_batch_sync(b);
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, ev0, ev1);
-            t.ms_per_step = ms / (float)trial_steps;
-            if (st == NW_OK && t.ms_per_step < best.ms_per_step) best = t;
-        }
+        for (int s = 0; s < 4 && st == NW_OK; ++s)
+            for (int c = 0; c < 2 && st == NW_OK; ++c) {
+                NwBatchTuning t = searches[s];
+                t.threads_per_block = threads[a];
+                t.cell_capacity = caps[c];
+                // a candidate the replicas cannot run (e.g. lists too large) is skipped
+                if (configure(b, t) != NW_OK) continue;
+                st = restore();
+                if (st == NW_OK) st = nw_batch_step(b, trial_steps);  // capture + warm
+                if (st == NW_OK) st = nw_batch_sync(b);
+                if (st == NW_ERR_CELL_OVERFLOW) {  // cells too small for this state: skipped
+                    st = NW_OK;
+                    continue;
+                }
+                if (st == NW_OK) st = restore();
+                if (st != NW_OK) break;
+                cudaEventRecord(ev0, b->stream);
+                st = nw_batch_step(b, trial_steps);
+                cudaEventRecord(ev1, b->stream);
+                if (st == NW_OK) st = nw_batch_sync(b);
+                if (st == NW_ERR_CELL_OVERFLOW) {
+                    st = NW_OK;
+                    continue;
+                }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, ev0, ev1);
+                t.ms_per_step = ms / (float)trial_steps;
+                if (st == NW_OK && t.ms_per_step < best.ms_per_step) best = t;
+            }
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
     if (st == NW_OK) st = configure(b, best.ms_per_step < INFINITY ? best : start);
     if (st == NW_OK) st = restore();
     b->tune.ms_per_step = best.ms_per_step < INFINITY ? best.ms_per_step : 0.0f;
     free_list(scratch);
+    if (st == NW_OK && best.ms_per_step < INFINITY) tune_cache_store(key, b->tune);
     if (st == NW_OK && chosen) *chosen = b->tune;
     return st;
 }

@@ -283,7 +283,7 @@ class NwBatchTuning(C.Structure):
     """include/nwgb_batch.h NwBatchTuning."""
 
     _fields_ = [("threads_per_block", _u32), ("strategy", C.c_int32), ("neighbor_skin", _f32),
-                ("ms_per_step", _f32)]
+                ("ms_per_step", _f32), ("cell_capacity", _u32)]
 
 
 _bp = C.c_void_p
@@ -304,6 +304,7 @@ BATCH_API = [
     ("nw_batch_get_tuning", C.c_int, [_bp, C.POINTER(NwBatchTuning)]),
     ("nw_batch_set_tuning", C.c_int, [_bp, C.POINTER(NwBatchTuning)]),
     ("nw_batch_autotune", C.c_int, [_bp, C.c_int, C.POINTER(NwBatchTuning)]),
+    ("nw_batch_tuning_class", C.c_int, [_bp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
 ]
 
 

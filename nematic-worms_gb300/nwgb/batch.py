@@ -99,11 +99,21 @@ class Batch:
         check(self.lib.nw_batch_get_tuning(self.h, C.byref(t)))
         return t
 
-    def set_tuning(self, threads_per_block: int, strategy: int, neighbor_skin: float) -> None:
-        t = NwBatchTuning(threads_per_block, strategy, neighbor_skin, 0.0)
+    def set_tuning(self, threads_per_block: int, strategy: int, neighbor_skin: float,
+                   cell_capacity: int = 0) -> None:
+        t = NwBatchTuning(threads_per_block, strategy, neighbor_skin, 0.0, cell_capacity)
         check(self.lib.nw_batch_set_tuning(self.h, C.byref(t)), "nw_batch_set_tuning")
 
     def autotune(self, trial_steps: int = 20) -> NwBatchTuning:
+        """Time the candidates and keep the fastest (cached for the batch's
+        class); trial_steps = 0 takes the cached tuning of the class."""
         t = NwBatchTuning()
         check(self.lib.nw_batch_autotune(self.h, trial_steps, C.byref(t)), "nw_batch_autotune")
         return t
+
+    @property
+    def tuning_class(self) -> tuple[int, int]:
+        """(bead-count class, packing class) keying the tuning cache."""
+        a, p = C.c_int(), C.c_int()
+        check(self.lib.nw_batch_tuning_class(self.h, C.byref(a), C.byref(p)))
+        return a.value, p.value

@@ -141,12 +141,45 @@ def test_autotune_keeps_state_and_picks_a_candidate(lib):
         t = b.autotune(trial_steps=5)
         assert t.threads_per_block in (128, 256, 512)
         assert t.strategy in (abi.NW_STRATEGY_VERLET, abi.NW_STRATEGY_CELL_LISTS)
+        assert t.cell_capacity in (8, 16)
         assert t.ms_per_step > 0
         assert b.step_index == 3
         for r in range(len(cfgs)):
             assert np.array_equal(b.get_array(r, abi.NW_POSITION), before[r])
         b.step(5)
         b.sync()
+        key = b.tuning_class
+    # a batch of the same class takes the cached tuning without timing
+    with nwgb.Batch(cfgs) as b2:
+        assert b2.tuning_class == key
+        t2 = b2.autotune(trial_steps=0)
+        assert (t2.threads_per_block, t2.strategy, t2.cell_capacity) == (t.threads_per_block, t.strategy,
+                                                                           t.cell_capacity)
+        assert t2.neighbor_skin == t.neighbor_skin and t2.ms_per_step == t.ms_per_step
+
+
+def test_tuning_cell_capacity(lib):
+    """Slots per list cell as a tuning axis: 8 and 16 give the same
+    trajectory (no cell overflows here); other values are rejected."""
+    import nwgb
+
+    cfgs, states = small_batch(lib, n=3, seed=4)
+    out = []
+    for cap in (8, 16):
+        with nwgb.Batch(cfgs) as b:
+            b.set_tuning(256, abi.NW_STRATEGY_VERLET, 0.3, cap)
+            assert b.tuning.cell_capacity == cap
+            for r, (pos, vel) in enumerate(states):
+                b.set_array(r, abi.NW_POSITION, pos)
+                b.set_array(r, abi.NW_VELOCITY, vel)
+            b.step(10)
+            b.sync()
+            out.append([b.get_array(r, abi.NW_POSITION) for r in range(len(cfgs))])
+            with pytest.raises(nwgb.NwError) as e:
+                b.set_tuning(256, abi.NW_STRATEGY_VERLET, 0.3, 12)
+            assert e.value.status == abi.NW_ERR_INVALID
+    for r in range(len(cfgs)):
+        assert np.array_equal(out[0][r], out[1][r])
 
 
 def test_batch_rejects_solvent_and_reports_nonfinite(lib):
