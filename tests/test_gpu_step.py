@@ -301,6 +301,38 @@ def test_graph_replay_is_bit_identical_to_direct_launches(lib, kind, strategy):
         assert np.array_equal(a[k], c[k]), k  # run twice: no races
 
 
+@pytest.mark.parametrize("graphs", [True, False])
+@pytest.mark.parametrize("strategy", STRATEGIES)
+def test_run_split_over_calls_is_bit_identical(lib, strategy, graphs):
+    """25 updates with SRD collisions at 0, 10 and 20 in one call, in three
+    calls of other SRD phases, and in three calls with the positions written
+    back from the host in between, give the same state bit for bit."""
+    import nwgb
+
+    cfg, pos, vel, tan = make_case("wca_srd", lib)
+    cfg.strategy = strategy
+
+    def run(splits, rewrite):
+        s = nwgb.System(cfg)
+        s.set_graphs(graphs)
+        s.set_array(abi.NW_POSITION, pos)
+        s.set_array(abi.NW_VELOCITY, vel)
+        s.set_array(abi.NW_TANGENT, tan)
+        for n in splits:
+            if rewrite:
+                s.set_array(abi.NW_POSITION, s.get_array(abi.NW_POSITION))
+            s.step(n, cfg.dt)
+        s.sync()
+        out = (s.get_array(abi.NW_POSITION), s.get_array(abi.NW_VELOCITY))
+        s.close()
+        return out
+
+    a = run([25], False)
+    assert len(a[0]) > cfg.n_beads
+    for x in (run([7, 9, 9], False), run([7, 9, 9], True)):
+        assert np.array_equal(a[0], x[0]) and np.array_equal(a[1], x[1])
+
+
 @pytest.mark.parametrize("strategy", STRATEGIES)
 def test_planar_system_carries_z(lib, strategy):
     """Two-dimensional WCA worms compute in the xy plane, with the two vector
