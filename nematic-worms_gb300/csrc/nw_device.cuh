@@ -357,13 +357,17 @@ __device__ __forceinline__ uint32_t srd_hash(const DevParams& P, float3 p, float
     uint32_t c[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
+        const uint32_t G = P.srd_grid[a];
+        if (G == 1u) {  // a single layer (the z axis of 2D systems): cell 0 in every mode
+            c[a] = 0u;
+            continue;
+        }
         float rel = t[a] - P.origin[a];
         if (P.bnd[a] == NW_PERIODIC) {
             if (rel >= P.box[a]) rel -= P.box[a];
             else if (rel < 0.0f) rel += P.box[a];
         }
-        const uint32_t G = P.srd_grid[a];
-        const int g = G == 1u ? 0 : floor_div(rel, P.srd_cell[a], P.srd_inv_cell[a]);
+        const int g = floor_div(rel, P.srd_cell[a], P.srd_inv_cell[a]);
         if (P.bnd[a] == NW_PERIODIC)
             c[a] = P.hash_mode == NW_HASH_MASK ? ((uint32_t)g & (G - 1u)) : wrap_mod(g, G);
         else

@@ -546,6 +546,7 @@ constexpr int kCollideWarps = 4;
 // 8 blocks of 4 warps resident per SM (27 KB of shared memory, 64 registers).
 constexpr uint32_t kWarpCap = 192;
 static_assert(kLaneCap <= kWarpCap, "a cell of the warp path fits the staging alone");
+static_assert(5 * ((kWarpCap + 31) / 32) <= 32, "a lane's slot-to-cell fields fit one register");
 
 __global__ void __launch_bounds__(kCollideWarps * 32, 8) srd_collide_kernel(const DevParams P, const StepBuffers S,
                                                                          uint32_t step_off, float dt_srd,
@@ -604,6 +605,10 @@ __global__ void __launch_bounds__(kCollideWarps * 32, 8) srd_collide_kernel(cons
         // is solvent k.  The bucket entries are loaded lane-strided (consecutive
         // cells' entries are consecutive in the buckets), each into its cell's
         // segment; then every lane orders its own cell's segment in shared memory.
+        // A lane visits the same slots (j0 + lane) in the three loops below, so
+        // the cell of each of its (at most kWarpCap / 32 = 6) slots is found once
+        // and kept in 5-bit fields of one register.
+        uint32_t qpack = 0;
 #pragma unroll 2
         for (uint32_t j0 = 0; j0 < rtotal; j0 += 32u) {
             const uint32_t j = j0 + lane, slot = base + (j < rtotal ? j : 0u);
@@ -613,6 +618,7 @@ __global__ void __launch_bounds__(kCollideWarps * 32, 8) srd_collide_kernel(cons
                 const uint32_t lq = __shfl_sync(0xffffffffu, loc, (int)(q + st));
                 if (lq <= slot) q += st;
             }
+            qpack |= q << (5u * (j0 >> 5));
             const uint32_t lq = __shfl_sync(0xffffffffu, loc, (int)q), nq = __shfl_sync(0xffffffffu, nbc, (int)q);
             const uint32_t bq = __shfl_sync(0xffffffffu, b0, (int)q), sq = __shfl_sync(0xffffffffu, s0, (int)q);
             if (j < rtotal) {
@@ -636,12 +642,7 @@ __global__ void __launch_bounds__(kCollideWarps * 32, 8) srd_collide_kernel(cons
         __syncwarp();
         for (uint32_t j0 = 0; j0 < rtotal; j0 += 32u) {
             const uint32_t j = j0 + lane, slot = base + (j < rtotal ? j : 0u);
-            uint32_t q = 0;  // the cell of slot, as above
-#pragma unroll
-            for (uint32_t st = 16; st; st >>= 1) {
-                const uint32_t lq = __shfl_sync(0xffffffffu, loc, (int)(q + st));
-                if (lq <= slot) q += st;
-            }
+            const uint32_t q = (qpack >> (5u * (j0 >> 5))) & 31u;  // the cell of slot
             const uint32_t gq = __shfl_sync(0xffffffffu, gdelta, (int)q);
             if (j < rtotal) {
                 const uint32_t id = s_id[w][j];
@@ -711,12 +712,7 @@ __global__ void __launch_bounds__(kCollideWarps * 32, 8) srd_collide_kernel(cons
         __syncwarp();
         for (uint32_t j0 = 0; j0 < rtotal; j0 += 32u) {
             const uint32_t j = j0 + lane, slot = base + (j < rtotal ? j : 0u);
-            uint32_t q = 0;  // the cell of slot, as above
-#pragma unroll
-            for (uint32_t st = 16; st; st >>= 1) {
-                const uint32_t lq = __shfl_sync(0xffffffffu, loc, (int)(q + st));
-                if (lq <= slot) q += st;
-            }
+            const uint32_t q = (qpack >> (5u * (j0 >> 5))) & 31u;  // the cell of slot
             const float3 uq = make_float3(__shfl_sync(0xffffffffu, u.x, (int)q), __shfl_sync(0xffffffffu, u.y, (int)q),
                                           __shfl_sync(0xffffffffu, u.z, (int)q));
             const float l1 = __shfl_sync(0xffffffffu, lam1, (int)q), saq = __shfl_sync(0xffffffffu, sa, (int)q);
