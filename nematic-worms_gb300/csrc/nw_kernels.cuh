@@ -572,8 +572,17 @@ __global__ void __launch_bounds__(256) srd_scatter_kernel(const DevParams P, con
 // One warp per SRD cell of the srd_big list (grid-stride over the list).
 __global__ void __launch_bounds__(128) srd_collide_big_kernel(const DevParams P, const StepBuffers S,
                                                               uint32_t step_off, float dt_srd, uint32_t buf_sel);
-constexpr uint32_t kSrdBigBlocks = 608;  // 4 blocks per SM
-constexpr uint32_t kLaneCap = 16;        // members of a cell collided by one lane of srd_collide_kernel
+// Tuning of the collision's two paths (overridable at compile time):
+// blocks of srd_collide_big_kernel, and the largest cell one lane of
+// srd_collide_kernel collides (larger cells go to the warp-per-cell kernel).
+#ifndef NW_SRD_BIG_BLOCKS
+#define NW_SRD_BIG_BLOCKS 912  // 6 blocks per SM (its shared memory allows 6, its registers 7)
+#endif
+#ifndef NW_SRD_LANE_CAP
+#define NW_SRD_LANE_CAP 16
+#endif
+constexpr uint32_t kSrdBigBlocks = NW_SRD_BIG_BLOCKS;
+constexpr uint32_t kLaneCap = NW_SRD_LANE_CAP;  // members of a cell collided by one lane of srd_collide_kernel
 constexpr uint32_t kBigWarps = 4;        // warps (cells at a time) per block of srd_collide_big_kernel
 constexpr uint32_t kBigCap = 384;        // members of a cell ordered exactly by srd_collide_big_kernel
 __global__ void srd_flip_kernel(uint32_t* scur);
