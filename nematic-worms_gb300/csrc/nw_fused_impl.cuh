@@ -220,11 +220,10 @@ __device__ __forceinline__ float vl_bound(const StepBuffers& S, unsigned long lo
 // tested against lj_rcut.  Pairs are summed in list order, which is the
 // cell-scan order of the build.  Neighbours are fetched in batches so that
 // the batch's index loads, then its position gathers, are in flight together:
-// four at a time, or six of the planar kernels, which gather only x and y
-// (8 bytes each, so the batch fits the register budget; measured 1.5 % per
-// step over batches of four).  A batch's pairs are evaluated without
-// branches, a pair beyond the cut-off (or past the end of the list, fetched
-// as bead i itself) adding 0 * dr.
+// four at a time, or six in the planar loop (verlet_force_planar), which
+// gathers only x and y (8 bytes each, so the batch fits the register budget).
+// A batch's pairs are evaluated without branches, a pair beyond the cut-off
+// (or past the end of the list, fetched as bead i itself) adding 0 * dr.
 template <int D>
 __device__ __forceinline__ float3 verlet_force(const DevParams& P, const StepBuffers& S,
                                                const float4* __restrict__ pos, uint32_t i, float3 r)
@@ -233,26 +232,6 @@ __device__ __forceinline__ float3 verlet_force(const DevParams& P, const StepBuf
     if (k > P.vl_cap) k = P.vl_cap;
     float3 f = zero3();
     const uint32_t* __restrict__ col = S.nbr + i;
-    if constexpr (D == 2) {
-        constexpr int kB = 6;
-        for (uint32_t m = 0; m < k; m += kB) {
-            uint32_t j[kB];
-#pragma unroll
-            for (int q = 0; q < kB; ++q) j[q] = m + q < k ? __ldg(col + (size_t)(m + q) * P.nb) : i;
-            float2 pj[kB];
-#pragma unroll
-            for (int q = 0; q < kB; ++q) pj[q] = __ldg(reinterpret_cast<const float2*>(pos + j[q]));
-#pragma unroll
-            for (int q = 0; q < kB; ++q) {
-                float3 dr = make_float3(pj[q].x - r.x, pj[q].y - r.y, 0.f);
-                min_image_near<D>(P, dr);
-                const float rr = dotv<D>(dr, dr);
-                const bool in = m + q < k && rr <= P.lj_rc2;
-                sub_scaled<D>(f, in ? wca_lj(P, rr) : 0.0f, dr);
-            }
-        }
-        return f;
-    }
     for (uint32_t m = 0; m < k; m += 4) {
         uint32_t j[4];
 #pragma unroll
@@ -263,6 +242,59 @@ __device__ __forceinline__ float3 verlet_force(const DevParams& P, const StepBuf
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             float3 dr = subv<D>(f3(pj[q]), r);
+            min_image_near<D>(P, dr);
+            const float rr = dotv<D>(dr, dr);
+            const bool in = m + q < k && rr <= P.lj_rc2;
+            sub_scaled<D>(f, in ? wca_lj(P, rr) : 0.0f, dr);
+        }
+    }
+    return f;
+}
+
+// The planar loop's list length and first batch of six entries, loaded
+// before the rebuild decision so that they travel with the bound's words;
+// entries past the list are masked by its length, and rows beyond the list
+// capacity (at least 4) are read as row 0.
+constexpr int kPlanarBatch = 6;
+struct PlanarHead {
+    uint32_t k;
+    uint32_t j[kPlanarBatch];
+};
+
+__device__ __forceinline__ PlanarHead planar_head(const DevParams& P, const StepBuffers& S, uint32_t i)
+{
+    PlanarHead h;
+    h.k = __ldg(S.nnb + i);
+#pragma unroll
+    for (int q = 0; q < kPlanarBatch; ++q) h.j[q] = __ldg(S.nbr + i + (size_t)((uint32_t)q < P.vl_cap ? q : 0) * P.nb);
+    return h;
+}
+
+// verlet_force of planar systems: x and y of six neighbours gathered per
+// batch (8 bytes each), the first batch from the head.
+__device__ __forceinline__ float3 verlet_force_planar(const DevParams& P, const StepBuffers& S,
+                                                      const float4* __restrict__ pos, uint32_t i, float3 r,
+                                                      const PlanarHead& h)
+{
+    constexpr int D = 2;
+    const uint32_t k = h.k > P.vl_cap ? P.vl_cap : h.k;
+    float3 f = zero3();
+    const uint32_t* __restrict__ col = S.nbr + i;
+    for (uint32_t m = 0; m < k; m += kPlanarBatch) {
+        uint32_t j[kPlanarBatch];
+        if (m == 0) {
+#pragma unroll
+            for (int q = 0; q < kPlanarBatch; ++q) j[q] = (uint32_t)q < k ? h.j[q] : i;
+        } else {
+#pragma unroll
+            for (int q = 0; q < kPlanarBatch; ++q) j[q] = m + q < k ? __ldg(col + (size_t)(m + q) * P.nb) : i;
+        }
+        float2 pj[kPlanarBatch];
+#pragma unroll
+        for (int q = 0; q < kPlanarBatch; ++q) pj[q] = __ldg(reinterpret_cast<const float2*>(pos + j[q]));
+#pragma unroll
+        for (int q = 0; q < kPlanarBatch; ++q) {
+            float3 dr = make_float3(pj[q].x - r.x, pj[q].y - r.y, 0.f);
             min_image_near<D>(P, dr);
             const float rr = dotv<D>(dr, dr);
             const bool in = m + q < k && rr <= P.lj_rc2;
@@ -328,7 +360,8 @@ __device__ __forceinline__ void vl_commit(const StepBuffers& S, unsigned long lo
 
 // Pair force of bead i for update n (reads the update-n buffers and list).
 // blk = the block's index among the blocks of its system.  D = 2: planar
-// WCA systems (REF_DEM systems are always D = 3).
+// WCA systems (REF_DEM systems are always D = 3); their loop's first batch
+// is loaded before the rebuild decision (planar_head).
 template <int CAP, bool kRef, int D>
 __device__ __forceinline__ float3 list_pair_force(const DevParams& P, const StepBuffers& S, unsigned long long n,
                                                   uint32_t i, uint32_t blk)
@@ -339,10 +372,15 @@ __device__ __forceinline__ float3 list_pair_force(const DevParams& P, const Step
     const float3 r = f3(pick2(S.pos2, cur)[i]);
     if (kRef) return ref_list_force<CAP>(P, pick2(S.pos2, cur), pick2(S.vel2, cur), pick2(S.tan2, cur), cnt, slots, i, r);
     if (P.vl_on) {
+        PlanarHead head{};
+        if constexpr (D == 2) head = planar_head(P, S, i);
         const float bound = vl_bound(S, n);
         const bool rebuild = !(bound <= P.vl_half_skin);  // a NaN bound rebuilds too
         if (blk == 0 && threadIdx.x == 0) vl_commit(S, n, rebuild, bound);
-        if (!rebuild) return verlet_force<D>(P, S, pick2(S.pos2, cur), i, r);
+        if (!rebuild) {
+            if constexpr (D == 2) return verlet_force_planar(P, S, pick2(S.pos2, cur), i, r, head);
+            else return verlet_force<D>(P, S, pick2(S.pos2, cur), i, r);
+        }
         return verlet_build_force<CAP, D>(P, S, pick2(S.pos2, cur), cnt, slots, i, r, pick2(S.hash2, cur)[i]);
     }
     return wca_list_force<CAP, D>(P, pick2(S.pos2, cur), cnt, slots, i, r, pick2(S.hash2, cur)[i]);
