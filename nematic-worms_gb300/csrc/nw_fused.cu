@@ -28,8 +28,8 @@ uint64_t launch_bead_list(const DevParams& P, const StepBuffers& B, uint32_t off
 {
     if (P.nb == 0 || !P.vl_on) return 0;
     const uint32_t blocks = cdiv32(P.nb, 256) < 608u ? cdiv32(P.nb, 256) : 608u;  // 4 blocks per SM
-    if (B.cap == 16) bead_list_kernel<16><<<blocks, 256, 0, s>>>(P, B, off);
-    else bead_list_kernel<8><<<blocks, 256, 0, s>>>(P, B, off);
+    if (B.cap == 16) launch_pdl(bead_list_kernel<16>, blocks, 256, 0, s, P, B, off);
+    else launch_pdl(bead_list_kernel<8>, blocks, 256, 0, s, P, B, off);
     return 1;
 }
 

@@ -19,6 +19,8 @@
 // order as with the sorted arrays, and runs are bit-identical.
 #pragma once
 
+#include <utility>
+
 #include "nw_fused.cuh"
 
 namespace nw {
@@ -35,6 +37,45 @@ __device__ __forceinline__ T* pick2(T* const (&a)[2], uint32_t k)
 __device__ __forceinline__ uint32_t* pick3(uint32_t* const (&a)[3], uint32_t k)
 {
     return k == 0u ? a[0] : (k == 1u ? a[1] : a[2]);
+}
+
+// Programmatic dependent launch: the step kernels are launched with the
+// stream-serialisation attribute relaxed, so that a kernel's blocks may be
+// scheduled while the previous kernel's last blocks still run.  Each step
+// kernel first waits (griddepcontrol.wait) until the previous kernel has
+// completed and its writes are visible, exactly the stream order, and then
+// lets the next launch begin.  Launched without the attribute both
+// instructions return at once.  NW_PDL=0 builds plain launches.
+#ifndef NW_PDL
+#define NW_PDL 1
+#endif
+__device__ __forceinline__ void pdl_enter()
+{
+#if NW_PDL
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
+
+template <class... KArgs, class... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), uint32_t grid, uint32_t block, size_t smem, cudaStream_t s,
+                       Args&&... args)
+{
+#if NW_PDL
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+#else
+    kernel<<<grid, block, smem, s>>>(std::forward<Args>(args)...);
+#endif
 }
 
 // Ascending bitonic sort of N (power of two) registers, fully unrolled.
@@ -565,6 +606,7 @@ __device__ __forceinline__ void pro_part(const DevParams& P, const StepBuffers& 
 template <int CAP>
 __global__ void __launch_bounds__(256) bead_list_kernel(const DevParams P, const StepBuffers S, uint32_t off)
 {
+    pdl_enter();
     const unsigned long long n = *S.step_base + off;
     if (vl_bound(S, n) <= P.vl_half_skin) return;
     const uint32_t out = (uint32_t)(n & 1ull);
@@ -585,6 +627,7 @@ template <int CAP, int MAXT, int D>
 __global__ void __launch_bounds__(MAXT) bead_pro_kernel(const DevParams P, const StepBuffers S, uint32_t off, float dt,
                                                         uint32_t fpb, uint32_t pflags)
 {
+    pdl_enter();
     const unsigned long long n = *S.step_base + off;
     const uint32_t i = blockIdx.x * fpb * P.L + threadIdx.x;
     const bool active = threadIdx.x < fpb * P.L && i < P.nb;
@@ -595,6 +638,7 @@ __global__ void __launch_bounds__(MAXT) bead_pro_kernel(const DevParams P, const
 template <int CAP, bool kRef, int D>
 __global__ void __launch_bounds__(256) bead_epi_kernel(const DevParams P, const StepBuffers S, uint32_t off)
 {
+    pdl_enter();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.nb) return;
     const unsigned long long n = *S.step_base + off;
@@ -612,6 +656,7 @@ template <int CAP, bool kRef, int MAXT, int D>
 __global__ void __launch_bounds__(MAXT, (MAXT == 256 && !kRef) ? NW_FUSED_MIN_BLOCKS : 1)
     bead_fused_kernel(const DevParams P, const StepBuffers S, uint32_t off, float dt, uint32_t fpb, uint32_t pflags)
 {
+    pdl_enter();
     const unsigned long long n = *S.step_base + off;
     const uint32_t i = blockIdx.x * fpb * P.L + threadIdx.x;
     const bool active = threadIdx.x < fpb * P.L && i < P.nb;
@@ -735,11 +780,11 @@ uint64_t bead_pro_d(const DevParams& P, const StepBuffers& B, uint32_t off, floa
     const bool big = threads > 256;  // filaments longer than 256 beads: one per block, up to 1024 threads
     const uint32_t pf = pro_flags(P);
     if (B.cap == 16) {
-        if (big) bead_pro_kernel<16, 1024, D><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb, pf);
-        else bead_pro_kernel<16, 256, D><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb, pf);
+        if (big) launch_pdl(bead_pro_kernel<16, 1024, D>, blocks, threads, smem, s, P, B, off, dt, fpb, pf);
+        else launch_pdl(bead_pro_kernel<16, 256, D>, blocks, threads, smem, s, P, B, off, dt, fpb, pf);
     } else {
-        if (big) bead_pro_kernel<8, 1024, D><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb, pf);
-        else bead_pro_kernel<8, 256, D><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb, pf);
+        if (big) launch_pdl(bead_pro_kernel<8, 1024, D>, blocks, threads, smem, s, P, B, off, dt, fpb, pf);
+        else launch_pdl(bead_pro_kernel<8, 256, D>, blocks, threads, smem, s, P, B, off, dt, fpb, pf);
     }
     return 1;
 }
@@ -759,13 +804,13 @@ uint64_t bead_epi_d(const DevParams& P, const StepBuffers& B, uint32_t off, cuda
     const bool ref = P.model == NW_MODEL_REF_DEM;
     if constexpr (D == 3) {
         if (ref) {
-            if (B.cap == 16) bead_epi_kernel<16, true, 3><<<blocks, 256, 0, s>>>(P, B, off);
-            else bead_epi_kernel<8, true, 3><<<blocks, 256, 0, s>>>(P, B, off);
+            if (B.cap == 16) launch_pdl(bead_epi_kernel<16, true, 3>, blocks, 256, 0, s, P, B, off);
+            else launch_pdl(bead_epi_kernel<8, true, 3>, blocks, 256, 0, s, P, B, off);
             return 1;
         }
     }
-    if (B.cap == 16) bead_epi_kernel<16, false, D><<<blocks, 256, 0, s>>>(P, B, off);
-    else bead_epi_kernel<8, false, D><<<blocks, 256, 0, s>>>(P, B, off);
+    if (B.cap == 16) launch_pdl(bead_epi_kernel<16, false, D>, blocks, 256, 0, s, P, B, off);
+    else launch_pdl(bead_epi_kernel<8, false, D>, blocks, 256, 0, s, P, B, off);
     return 1;
 }
 
@@ -781,8 +826,8 @@ uint64_t bead_fused_d(const DevParams& P, const StepBuffers& B, uint32_t off, fl
     const uint32_t pf = pro_flags(P);
 #define NW_FUSED(CAPV, REFV)                                                                                   \
     do {                                                                                                       \
-        if (big) bead_fused_kernel<CAPV, REFV, 1024, D><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb, pf); \
-        else bead_fused_kernel<CAPV, REFV, 256, D><<<blocks, threads, smem, s>>>(P, B, off, dt, fpb, pf);      \
+        if (big) launch_pdl(bead_fused_kernel<CAPV, REFV, 1024, D>, blocks, threads, smem, s, P, B, off, dt, fpb, pf); \
+        else launch_pdl(bead_fused_kernel<CAPV, REFV, 256, D>, blocks, threads, smem, s, P, B, off, dt, fpb, pf);      \
     } while (0)
     if constexpr (D == 3) {
         if (ref) {
