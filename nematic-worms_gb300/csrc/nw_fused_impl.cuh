@@ -685,12 +685,14 @@ __global__ void __launch_bounds__(MAXT, MAXT == 256 ? 6 : 1) batch_kernel(const 
     const ReplicaSlot* e = table + r;
     if (MODE == kBatchList) {
         // leave before staging the parameter block unless this replica rebuilds
-        if (!e->P.vl_on || !S0.vstate) return;
+        // (two round trips: the step counter beside the replica index, then the
+        // replica's bound beside its skin)
+        if (!S0.vstate) return;
         const unsigned long long n0 = *S0.step_base + off;
         const uint32_t* vs = S0.vstate + 8u * r;
         const float bound = __uint_as_float(vs[(uint32_t)((n0 + 1ull) & 1ull)]) +
                             __uint_as_float(vs[2u + (uint32_t)(n0 % 3ull)]);
-        if (bound <= e->P.vl_half_skin) return;
+        if (!e->P.vl_on || bound <= e->P.vl_half_skin) return;
     }
     {
         const uint32_t* src = reinterpret_cast<const uint32_t*>(&e->P);
