@@ -286,6 +286,12 @@ void free_all(nw_system* s)
     s->obs_ws = s->obs_msd = s->obs_srd = nullptr;
     s->obs_ws_bytes = s->obs_msd_bytes = s->obs_srd_bytes = 0;
     s->obs_msd_on = false;
+    if (s->aux) cudaStreamDestroy(s->aux);
+    if (s->state_ev) cudaEventDestroy(s->state_ev);
+    if (s->aux_done) cudaEventDestroy(s->aux_done);
+    s->aux = nullptr;
+    s->state_ev = s->aux_done = nullptr;
+    s->state_ev_valid = false;
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     s->own_stream = nullptr;
 }
@@ -348,6 +354,18 @@ uint64_t enqueue_steps(nw_system* s, int nsteps, float dt, uint64_t first_step, 
     const uint32_t gap = s->cfg.srd_gap ? s->cfg.srd_gap : 1u;
     const float dt_srd = dt * (float)gap;
     uint64_t launches = 0;
+    // positions and velocities of the last update are final here (an event
+    // node of the graph under capture); single updates only, the round trip of
+    // a caller that feeds and reads the state every update (longer calls keep
+    // their graphs free of the extra node)
+    bool state_marked = nsteps != 1 || prof;
+    auto mark_state = [&]() {
+        cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(s->stream, &cst);
+        cudaEventRecordWithFlags(s->state_ev, s->stream,
+                                 cst == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault);
+        state_marked = true;
+    };
     if (!s->lists) {
         for (int j = 0; j < nsteps; ++j) {
             launches += enqueue_bead_step(P, s->B, s->nchunks, (uint32_t)j, dt, s->stream, prof);
@@ -377,6 +395,8 @@ uint64_t enqueue_steps(nw_system* s, int nsteps, float dt, uint64_t first_step, 
             const bool srd_now = srd && ((first_step + (uint64_t)j) % gap) == 0;
             if (srd_now && wca) collide((uint32_t)j);
             if (j == nsteps - 1 || (srd_now && !wca)) {
+                // WCA: the last update's pair pass changes forces only
+                if (j == nsteps - 1 && wca && !state_marked) mark_state();
                 NW_MARK("bead_epi");
                 launches += launch_bead_epi(P, s->B, (uint32_t)j, s->stream);
                 if (srd_now && !wca) collide((uint32_t)j);
@@ -392,6 +412,7 @@ uint64_t enqueue_steps(nw_system* s, int nsteps, float dt, uint64_t first_step, 
             }
         }
     }
+    if (!state_marked) mark_state();
     if (prof) prof->mark("advance_step");
     advance_step_kernel<<<1, 1, 0, s->stream>>>(s->B.step_base, (unsigned long long)nsteps);
     if (prof) prof->end();
@@ -456,6 +477,17 @@ enum class Dir { ToDevice, ToHost };
 // velocity arrays are beads [0, nb) then solvent [nb, nb + ns) in two stores.
 nw_status transfer(nw_system* s, int array, void* host, uint32_t start, uint32_t count, Dir dir, bool wait = true)
 {
+    // an asynchronous read of positions or velocities right after a step
+    // starts on aux once they are final (state_ev), beside the step's pair
+    // pass; the engine's stream then waits for it
+    const bool early = dir == Dir::ToHost && !wait && s->state_ev_valid &&
+                       (array == NW_POSITION || array == NW_VELOCITY);
+    if (dir == Dir::ToDevice) s->state_ev_valid = false;
+    cudaStream_t cs = s->stream;
+    if (early) {
+        if (cudaStreamWaitEvent(s->aux, s->state_ev, 0) != cudaSuccess) return cuda_status(cudaGetLastError());
+        cs = s->aux;
+    }
     const uint32_t cur = cur_buffer(s);
     const StepBuffers& B = s->B;
     void* bead_ptr = nullptr;
@@ -529,7 +561,7 @@ nw_status transfer(nw_system* s, int array, void* host, uint32_t start, uint32_t
         const uint64_t a = start, b = end < nbead ? end : nbead;
         char* d = static_cast<char*>(bead_ptr) + a * elem;
         e = dir == Dir::ToDevice ? cudaMemcpyAsync(d, h, (b - a) * elem, cudaMemcpyHostToDevice, s->stream)
-                                 : cudaMemcpyAsync(h, d, (b - a) * elem, cudaMemcpyDeviceToHost, s->stream);
+                                 : cudaMemcpyAsync(h, d, (b - a) * elem, cudaMemcpyDeviceToHost, cs);
         h += (b - a) * elem;
     }
     // solvent part
@@ -537,7 +569,11 @@ nw_status transfer(nw_system* s, int array, void* host, uint32_t start, uint32_t
         const uint64_t a = start > nbead ? start : nbead, b = end;
         char* d = static_cast<char*>(solv_ptr) + (a - nbead) * elem;
         e = dir == Dir::ToDevice ? cudaMemcpyAsync(d, h, (b - a) * elem, cudaMemcpyHostToDevice, s->stream)
-                                 : cudaMemcpyAsync(h, d, (b - a) * elem, cudaMemcpyDeviceToHost, s->stream);
+                                 : cudaMemcpyAsync(h, d, (b - a) * elem, cudaMemcpyDeviceToHost, cs);
+    }
+    if (e == cudaSuccess && early) {
+        e = cudaEventRecord(s->aux_done, s->aux);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, s->aux_done, 0);
     }
     if (e == cudaSuccess && wait) e = cudaStreamSynchronize(s->stream);
     if (dir == Dir::ToDevice) {
@@ -595,6 +631,16 @@ nw_status nw_create(const NwConfig* cfg, nw_system** out)
     s->nchunks = (s->ncells + kChunk - 1) / kChunk;
     s->srd_ncells = cfg->srd_enabled ? cfg->srd_grid[0] * cfg->srd_grid[1] * cfg->srd_grid[2] : 0u;
     s->srd_nchunks = (s->srd_ncells + kChunk - 1) / kChunk;
+    if (cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->state_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->aux_done, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        if (s->aux) cudaStreamDestroy(s->aux);
+        if (s->state_ev) cudaEventDestroy(s->state_ev);
+        cudaStreamDestroy(s->own_stream);
+        delete s;
+        return NW_ERR_CUDA;
+    }
     StepBuffers& B = s->B;
     std::memset(&B, 0, sizeof(B));
     const size_t nb = s->nb, ns = s->ns, C = s->ncells;
@@ -749,6 +795,7 @@ nw_status nw_set_config(nw_system* s, const NwConfig* cfg)
     for (int a = 0; a < 3; ++a)
         if (Pn.lgrid[a] != Po.lgrid[a]) return NW_ERR_INVALID;
     s->cfg = *cfg;
+    s->state_ev_valid = false;
     s->vl_dirty = true;  // radii or the box may have changed
     s->hash_for = ~0ull;
     s->sorted_for = ~0ull;
@@ -800,6 +847,7 @@ nw_status nw_get_array_async(nw_system* s, int array, void* host, uint32_t start
 nw_status nw_device_array(nw_system* s, int array, void** dptr)
 {
     if (!s || !dptr) return NW_ERR_INVALID;
+    s->state_ev_valid = false;  // the caller may write through the pointer
     const uint32_t cur = cur_buffer(s);
     const StepBuffers& B = s->B;
     void* p = nullptr;
@@ -919,6 +967,7 @@ nw_status nw_step(nw_system* s, int nsteps, float dt)
     s->scur ^= collision_parity(s, s->step, nsteps);
     s->step += (uint64_t)nsteps;
     if (lazy_tangents(s)) s->tan_stale = true;
+    s->state_ev_valid = nsteps == 1;  // the graphs of single updates record state_ev
     return NW_OK;
 }
 
@@ -974,6 +1023,7 @@ nw_status nw_set_step(nw_system* s, uint64_t step)
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     if (e == cudaSuccess) {
         s->step = step;
+        s->state_ev_valid = false;
         s->lists_dirty = true;
         s->vl_dirty = true;
         s->sorted_for = ~0ull;
@@ -1006,6 +1056,7 @@ nw_status nw_srd_collide(nw_system* s, float dt_srd, const float shift[3])
     s->last_launches = enqueue_srd(P, s->B, s->srd_nchunks, 0u, dt_srd, 0, make_float3(shift[0], shift[1], shift[2]),
                                    s->stream, nullptr, cur_buffer(s));
     s->scur ^= 1u;
+    s->state_ev_valid = false;
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     return cuda_status(e);
@@ -1096,6 +1147,7 @@ nw_status nw_profile_steps(nw_system* s, int nsteps, float dt, NwKernelTime* out
     if (e != cudaSuccess) return cuda_status(e);
     Prof prof;
     prof.stream = s->stream;
+    s->state_ev_valid = false;  // the profiled launches record no state event
     s->last_launches = enqueue_steps(s, nsteps, dt, s->step, &prof);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);

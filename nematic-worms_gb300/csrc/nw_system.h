@@ -36,6 +36,13 @@ struct nw_system {
     bool tan_stale = false;       // tangents not stored by the step: computed when read
     std::vector<GraphEntry> graphs;
     uint64_t last_launches = 0;
+    // early read-back: the step graphs record state_ev once the positions and
+    // velocities of their last update are final (before its pair pass), so
+    // an asynchronous read of them runs on aux beside the rest of the step;
+    // valid while nothing else has been enqueued that writes them
+    cudaStream_t aux = nullptr;
+    cudaEvent_t state_ev = nullptr, aux_done = nullptr;
+    bool state_ev_valid = false;
     std::vector<void*> allocs;
     // defect search workspace (nw_defects.cu): bounds, counters and marked
     // cells (fixed), the per-cell sums (grown on demand), a pinned host copy
