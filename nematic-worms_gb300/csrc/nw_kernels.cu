@@ -477,7 +477,14 @@ __global__ void __launch_bounds__(256) srd_hash_kernel(const DevParams P, const 
     __shared__ float s_shift[3];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < P.ntotal;
+    const bool bead = i < P.nb;
+    // the step counter and the solvent buffer index side by side, then the
+    // particle's position, all before the shift's barrier
     const unsigned long long step = *S.step_base + step_off;
+    const uint32_t sc = *S.scur;
+    const uint32_t cur = buf_sel < 2u ? buf_sel : (uint32_t)(step & 1ull);
+    float4 p4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (valid) p4 = bead ? S.pos2[cur][i] : S.spos2[sc][i - P.nb];
     if (shift_from_step) {
         if (threadIdx.x == 0) {
             const float3 d = srd_shift_of(P, step);
@@ -488,11 +495,8 @@ __global__ void __launch_bounds__(256) srd_hash_kernel(const DevParams P, const 
         __syncthreads();
         shift = make_float3(s_shift[0], s_shift[1], s_shift[2]);
     }
-    const uint32_t cur = buf_sel < 2u ? buf_sel : (uint32_t)(step & 1ull);
-    const bool bead = i < P.nb;
     uint32_t h = 0, key = 0xffffffffu;  // no cell hash reaches 2^31 - 1 with the bead bit set
     if (valid) {
-        const float4 p4 = bead ? S.pos2[cur][i] : S.spos2[*S.scur][i - P.nb];
         h = srd_hash(P, f3(p4), shift);
         S.srd_hash[i] = h;
         key = h | (bead ? 0x80000000u : 0u);
