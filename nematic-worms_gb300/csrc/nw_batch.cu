@@ -6,7 +6,7 @@
 // Verlet lists are concatenations of per-replica tables (offsets in each
 // replica's ReplicaSlot).  A launch's block b serves replica block_rep[b],
 // whose parameter block it copies into shared memory before running the same
-// pro / epi / fused step bodies as a single system (nw_fused.cu).
+// pro / epi / fused step bodies as a single system (nw_fused_impl.cuh).
 #include <cmath>
 #include <cstring>
 #include <mutex>

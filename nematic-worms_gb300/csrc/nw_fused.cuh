@@ -1,4 +1,5 @@
-// nw_fused.cuh — launchers of the cell-list step path (nw_fused.cu).
+// nw_fused.cuh — launchers of the cell-list step path (nw_fused.cu, nw_fused_planar.cu;
+// device code in nw_fused_impl.cuh).
 #pragma once
 
 #include "nw_kernels.cuh"

@@ -26,7 +26,6 @@
 namespace nw {
 namespace {
 
-
 // Buffer k of a double / triple buffer by selects rather than an indexed
 // load: a StepBuffers copy in registers (the batch kernel's) stays there.
 template <class T>

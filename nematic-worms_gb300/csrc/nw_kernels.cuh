@@ -9,7 +9,7 @@
 //   stable_gather   order every bucket by index (the stable sort) and
 //                   gather positions (+ velocities and tangents) in cell order
 //   pair_*          pair forces over the 3x3(x3) neighbour cells
-// The cell-list and Verlet strategies (nw_fused.cu) run one fused kernel
+// The cell-list and Verlet strategies (nw_fused_impl.cuh) run one fused kernel
 // per step instead.  Every srd_gap steps an SRD collision adds seven:
 //   srd_hash, chunk_sum and scan_cells (bead and solvent buckets side by
 //   side), srd_scatter, srd_collide, srd_collide_big, srd_flip.
