@@ -45,6 +45,8 @@ REPO = Path(__file__).resolve().parent
 sys.path.insert(0, str(REPO / "nematic-worms_gb300"))
 
 GAP = 10
+GRAPH_STEPS = 100  # updates per step call (one CUDA graph each): whole SRD periods
+assert GRAPH_STEPS % GAP == 0
 REPEATS = 3
 PEAKS_FILE = REPO / "MEASURED_PEAKS.json"
 TRAFFIC_FILE = REPO / "profiles" / "traffic_per_unit.txt"
@@ -377,7 +379,7 @@ def strategies_block(cfg, pos, vel, warmup, steps, stream):
     from nwgb import abi
 
     out = {}
-    chunk = GAP if cfg.srd_enabled else 10
+    chunk = GRAPH_STEPS
     for name, strat in (("sorted", abi.NW_STRATEGY_SORTED), ("cell_lists", abi.NW_STRATEGY_CELL_LISTS),
                         ("verlet", abi.NW_STRATEGY_VERLET)):
         c = cfg.copy()
@@ -537,7 +539,7 @@ def run_ours(args):
     sysm.set_array(abi.NW_VELOCITY, vel)
     sysm.zero_forces()
 
-    chunk = GAP if cfg.srd_enabled else 10
+    chunk = GRAPH_STEPS
     sched = warm_and_prepare(sysm, cfg, args.warmup, args.steps, chunk)
     blob = sysm.checkpoint()
     clocks = ClockSampler(local)
