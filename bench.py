@@ -590,7 +590,7 @@ def run_ours(args):
     e2e_value, _ = job_rate(dist, 1e3 * e2e_s, nb * e2e_steps, device="cuda")
 
     # ---- per-kernel device time (events around every launch) ---------------------------
-    prof = sysm.profile(2 * chunk, cfg.dt)
+    prof = sysm.profile(2 * GAP, cfg.dt)
     sysm.sync()
     dom = max((k for k in prof if k != "advance_step"), key=lambda k: prof[k][0])
     dom_ms = prof[dom][0] / prof[dom][1]
