@@ -92,7 +92,10 @@ typedef enum { NW_SRD_THERMO_NONE = 0, NW_SRD_THERMO_REF_LAB = 1, NW_SRD_THERMO_
 typedef struct NwConfig {
     uint32_t abi_version;      /* must be NW_ABI_VERSION */
     int32_t  model;            /* nw_model */
-    int32_t  dim;              /* 2: noise and SRD shift have no z part; 3: full 3D */
+    int32_t  dim;              /* 2: noise and SRD shift have no z part, and WCA_WORMS
+                                  systems compute in the xy plane (bead z and z velocity
+                                  carried unchanged, forces with z = 0, as the archived
+                                  two-component kernels); 3: full 3D */
     uint32_t num_filaments;
     uint32_t filament_size;    /* beads per filament, >= 1 */
     uint32_t grid[3];          /* bead cell grid */
