@@ -359,11 +359,16 @@ uint64_t enqueue_steps(nw_system* s, int nsteps, float dt, uint64_t first_step, 
     // a caller that feeds and reads the state every update (longer calls keep
     // their graphs free of the extra node)
     bool state_marked = nsteps != 1 || prof;
+    s->enqueued_state_ev = false;
     auto mark_state = [&]() {
         cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
-        cudaStreamIsCapturing(s->stream, &cst);
-        cudaEventRecordWithFlags(s->state_ev, s->stream,
-                                 cst == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault);
+        const bool ok =
+            cudaStreamIsCapturing(s->stream, &cst) == cudaSuccess &&
+            cudaEventRecordWithFlags(s->state_ev, s->stream, cst == cudaStreamCaptureStatusActive
+                                                                 ? cudaEventRecordExternal
+                                                                 : cudaEventRecordDefault) == cudaSuccess;
+        if (!ok) cudaGetLastError();  // no early read-back after this call
+        s->enqueued_state_ev = ok;
         state_marked = true;
     };
     if (!s->lists) {
@@ -930,7 +935,7 @@ static cudaError_t find_graph(nw_system* s, int nsteps, float dt, uint64_t first
     e = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return e;
-    s->graphs.push_back({nsteps, bits, phase, s->version, exec, launches});
+    s->graphs.push_back({nsteps, bits, phase, s->version, exec, launches, s->enqueued_state_ev});
     *out = &s->graphs.back();
     return cudaSuccess;
 }
@@ -959,15 +964,19 @@ nw_status nw_step(nw_system* s, int nsteps, float dt)
         if (e != cudaSuccess) return cuda_status(e);
         e = cudaGraphLaunch(hit->exec, s->stream);
         s->last_launches = hit->launches;
+        s->state_ev_valid = hit->state_ev;
     } else {
         s->last_launches = enqueue_steps(s, nsteps, dt, s->step);
+        s->state_ev_valid = s->enqueued_state_ev;
         e = cudaGetLastError();
     }
-    if (e != cudaSuccess) return cuda_status(e);
+    if (e != cudaSuccess) {
+        s->state_ev_valid = false;
+        return cuda_status(e);
+    }
     s->scur ^= collision_parity(s, s->step, nsteps);
     s->step += (uint64_t)nsteps;
     if (lazy_tangents(s)) s->tan_stale = true;
-    s->state_ev_valid = nsteps == 1;  // the graphs of single updates record state_ev
     return NW_OK;
 }
 

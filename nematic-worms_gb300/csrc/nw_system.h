@@ -13,6 +13,7 @@ struct GraphEntry {
     uint64_t version;
     cudaGraphExec_t exec;
     uint64_t launches;
+    bool state_ev;  // the graph records nw_system::state_ev
 };
 
 struct nw_system {
@@ -43,6 +44,7 @@ struct nw_system {
     cudaStream_t aux = nullptr;
     cudaEvent_t state_ev = nullptr, aux_done = nullptr;
     bool state_ev_valid = false;
+    bool enqueued_state_ev = false;  // the last enqueue_steps recorded state_ev
     std::vector<void*> allocs;
     // defect search workspace (nw_defects.cu): bounds, counters and marked
     // cells (fixed), the per-cell sums (grown on demand), a pinned host copy
